@@ -1,0 +1,261 @@
+// Batched gradient for logistic-likelihood models that share one design
+// matrix across all chains (logistic regression, regularised horseshoe).
+//
+// For C chains with coefficient rows B[c] = (b0, beta_1..K) the likelihood
+// part of log_prob_grad is
+//     eta[n,c] = b0_c + X[n,:] . beta_c                     (X . B^T)
+//     lp_c    += sum_n y_n eta[n,c] - log1p_exp(eta[n,c])
+//     r[n,c]   = y_n - inv_logit(eta[n,c])
+//     grad_c   = (sum_n r[n,c], X^T r[:,c])                 (R^T . X)
+// -- two contractions with an elementwise step between them, which is what
+// Stan Math's reverse sweep over the bernoulli_logit / GLM node computes for
+// one chain at a time (contract of log_prob_grad, src/cmdstan/
+// command_helper.hpp:589-593).  The model-specific parts (coefficients from
+// the unconstrained point, priors, Jacobians, chain rule to z / lambda / tau
+// for the horseshoe) run per chain in stage_request / reduce_gradient.
+//
+// Row blocks are split over S CTAs per chain tile; each CTA writes its
+// partial sums to [S][C] / [S][C][K+1] buffers which reduce_gradient sums in
+// a fixed order, so results are bitwise reproducible run to run.
+#pragma once
+#include "device_models.cuh"
+
+namespace gnuts {
+
+struct GradOut {
+  int kind;     // MK_LOGISTIC or MK_HORSESHOE
+  int prec;     // GNUTS_PRECISION_*
+  int C, K, S;  // chains, predictors, row splits
+  int rows_per_split;
+  double* coef64;   // [C][K+1]
+  float* coef32;    // [C][K+1]
+  double* part_lp;  // [S][C]
+  double* part_g;   // [S][C][K+1]
+  const int* done_count;
+  int C_total;
+  void* tc;         // tensor-core path state (grad_tc.cu)
+};
+
+inline bool batched_supported(const DevModel& M) {
+  return M.kind == MK_LOGISTIC || M.kind == MK_HORSESHOE;
+}
+
+// ---------------------------------------------------------------- staging
+// coefficient row of chain c from its unconstrained position q
+__device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& M, int c, const double* q,
+                                              int lane) {
+  const int K = M.K;
+  double* o64 = G.coef64 + (size_t)c * (K + 1);
+  float* o32 = G.coef32 ? G.coef32 + (size_t)c * (K + 1) : nullptr;
+  if (M.kind == MK_LOGISTIC) {
+    for (int i = lane; i <= K; i += 32) {
+      double v = q[i];
+      o64[i] = v;
+      if (o32) o32[i] = (float)v;
+    }
+  } else {  // horseshoe: beta = z .* lambda_tilde * tau
+    double tau = exp(q[K + 1]), caux = exp(q[2 * K + 2]);
+    double c2 = M.slab_scale * M.slab_scale * caux;
+    if (lane == 0) {
+      o64[0] = q[0];
+      if (o32) o32[0] = (float)q[0];
+    }
+    for (int d = lane; d < K; d += 32) {
+      double lam = exp(q[K + 2 + d]);
+      double l2 = lam * lam;
+      double lamt = sqrt(c2 * l2 / (c2 + tau * tau * l2));
+      double b = q[1 + d] * lamt * tau;
+      o64[1 + d] = b;
+      if (o32) o32[1 + d] = (float)b;
+    }
+  }
+}
+
+// sum the partials of chain c, add priors / Jacobian, write grad, return lp
+__device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevModel& M, int c, const double* q,
+                                                  double* g, int lane) {
+  const int K = M.K, S = G.S, C = G.C;
+  double lp = 0;
+  for (int s = lane; s < S; s += 32) lp += G.part_lp[(size_t)s * C + c];
+  lp = wsum(lp);
+  // likelihood gradient wrt (b0, beta) into g[0..K] (fixed summation order over s)
+  if (M.kind == MK_LOGISTIC) {
+    double pri = 0;
+    for (int i = lane; i <= K; i += 32) {
+      double t = 0;
+      for (int s = 0; s < S; ++s) t += G.part_g[((size_t)s * C + c) * (K + 1) + i];
+      double v = q[i];
+      if (i == 0) {
+        g[0] = t - v / 6.25;
+        pri += -0.5 * (v / 2.5) * (v / 2.5);
+      } else {
+        g[i] = t - v;
+        pri += -0.5 * v * v;
+      }
+    }
+    return lp + wsum(pri);
+  }
+  // horseshoe
+  const double nu = M.slab_df, ssl = M.slab_scale, sg = M.scale_global;
+  double lt = q[K + 1], tau = exp(lt), lc = q[2 * K + 2], caux = exp(lc);
+  double c2 = ssl * ssl * caux;
+  double pri = 0, glt = 0, glc = 0;
+  for (int d = lane; d < K; d += 32) {
+    double t = 0;
+    for (int s = 0; s < S; ++s) t += G.part_g[((size_t)s * C + c) * (K + 1) + 1 + d];
+    double z = q[1 + d];
+    double ll = q[K + 2 + d];
+    double lam = exp(ll);
+    double l2 = lam * lam;
+    double den = c2 + tau * tau * l2;
+    double a = c2 / den, bt = tau * tau * l2 / den;
+    double lamt = sqrt(c2 * l2 / den);
+    double beta = z * lamt * tau;
+    double gbd = t * beta;
+    pri += -0.5 * z * z - log1p(l2) + ll;
+    g[1 + d] = t * lamt * tau - z;
+    g[K + 2 + d] = gbd * a - 2.0 * l2 / (1.0 + l2) + 1.0;
+    glt += gbd * (1.0 - bt);
+    glc += gbd * 0.5 * bt;
+  }
+  pri = wsum(pri);
+  glt = wsum(glt);
+  glc = wsum(glc);
+  double b0 = q[0];
+  double ts = tau / sg;
+  double t0 = 0;
+  for (int s = lane; s < S; s += 32) t0 += G.part_g[((size_t)s * C + c) * (K + 1)];
+  t0 = wsum(t0);
+  lp += pri - 0.5 * (b0 / 2.5) * (b0 / 2.5) - log1p(ts * ts) + (-0.5 * nu - 1.0) * lc - 0.5 * nu / caux + lt + lc;
+  if (lane == 0) {
+    g[0] = t0 - b0 / 6.25;
+    g[K + 1] = glt - 2.0 * ts * ts / (1.0 + ts * ts) + 1.0;
+    g[2 * K + 2] = glc + (-0.5 * nu - 1.0) + 0.5 * nu / caux + 1.0;
+  }
+  return lp;
+}
+
+// ---------------------------------------------------------------- SIMT contraction
+// T = double (FP64 reference path) or float (FP32 CUDA-core path); the lp
+// sum is always accumulated in FP64.
+constexpr int GLM_CT = 16;   // chains per CTA
+constexpr int GLM_RB = 16;   // rows per block
+constexpr int GLM_KC = 128;  // predictor chunk
+constexpr int GLM_THREADS = 256;
+// NKC = predictor chunks held in registers: 1 for K <= 128, 8 for K <= 1024
+template <class T, int NKC>
+__global__ void __launch_bounds__(GLM_THREADS) k_glm_simt(GradOut G, DevModel M) {
+  if (G.done_count && *G.done_count >= G.C_total) return;
+  const int K = M.K;
+  const int c0 = blockIdx.x * GLM_CT;
+  const int split = blockIdx.y;
+  const int row_begin = split * G.rows_per_split;
+  const int row_end = min(M.N, row_begin + G.rows_per_split);
+  const int t = threadIdx.x;
+  const T* X = nullptr;
+  if constexpr (sizeof(T) == 8) X = (const T*)M.X; else X = (const T*)M.Xf;
+  const T* coef;
+  if constexpr (sizeof(T) == 8) coef = (const T*)G.coef64; else coef = (const T*)G.coef32;
+
+  __shared__ T xs[GLM_RB][GLM_KC + 1];
+  __shared__ T cs[GLM_CT][GLM_KC + 1];
+  __shared__ T rs[GLM_CT][GLM_RB];
+  __shared__ double lps[GLM_THREADS];
+
+  // eta / residual ownership: thread t -> (row t / CT, chain t % CT)
+  const int er = t / GLM_CT, ec = t % GLM_CT;
+  double lp_acc = 0;
+  T gacc[NKC][GLM_CT];
+#pragma unroll
+  for (int j = 0; j < NKC; ++j)
+#pragma unroll
+    for (int c = 0; c < GLM_CT; ++c) gacc[j][c] = 0;
+  T g0acc = 0;  // intercept gradient (thread ec handles chain ec when t < CT)
+  const int nkc = min(NKC, (K + GLM_KC - 1) / GLM_KC);
+
+  for (int r0 = row_begin; r0 < row_end; r0 += GLM_RB) {
+    // ---- eta
+    T eta = 0;
+    for (int kc = 0; kc < nkc; ++kc) {
+      const int k0 = kc * GLM_KC;
+      __syncthreads();
+      for (int i = t; i < GLM_RB * GLM_KC; i += GLM_THREADS) {
+        int rr = i / GLM_KC, kk = i % GLM_KC;
+        int n = r0 + rr, k = k0 + kk;
+        xs[rr][kk] = (n < row_end && k < K) ? X[(size_t)n * K + k] : T(0);
+      }
+      for (int i = t; i < GLM_CT * GLM_KC; i += GLM_THREADS) {
+        int cc = i / GLM_KC, kk = i % GLM_KC;
+        int c = c0 + cc, k = k0 + kk;
+        cs[cc][kk] = (c < G.C && k < K) ? coef[(size_t)c * (K + 1) + 1 + k] : T(0);
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int kk = 0; kk < GLM_KC; ++kk) eta += xs[er][kk] * cs[ec][kk];
+    }
+    {
+      const int n = r0 + er, c = c0 + ec;
+      T r = 0;
+      if (n < row_end && c < G.C) {
+        double e = (double)eta + (double)coef[(size_t)c * (K + 1)];
+        int y = M.yi[n];
+        lp_acc += y * e - log1p_exp(e);
+        r = (T)(y - inv_logit(e));
+      }
+      rs[ec][er] = r;
+    }
+    __syncthreads();
+    if (t < GLM_CT) {
+#pragma unroll
+      for (int rr = 0; rr < GLM_RB; ++rr) g0acc += rs[t][rr];
+    }
+    // ---- gradient: thread t owns predictor k = kc*KC + t (t < KC)
+#pragma unroll
+    for (int kc = 0; kc < NKC; ++kc) {
+      if (kc >= nkc) break;
+      const int k0 = kc * GLM_KC;
+      if (nkc > 1) {
+        __syncthreads();
+        for (int i = t; i < GLM_RB * GLM_KC; i += GLM_THREADS) {
+          int rr = i / GLM_KC, kk = i % GLM_KC;
+          int n = r0 + rr, k = k0 + kk;
+          xs[rr][kk] = (n < row_end && k < K) ? X[(size_t)n * K + k] : T(0);
+        }
+        __syncthreads();
+      }
+      if (t < GLM_KC) {
+#pragma unroll
+        for (int rr = 0; rr < GLM_RB; ++rr) {
+          T x = xs[rr][t];
+#pragma unroll
+          for (int c = 0; c < GLM_CT; ++c) gacc[kc][c] += rs[c][rr] * x;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // ---- write partials
+  lps[t] = lp_acc;
+  __syncthreads();
+  if (t < GLM_CT) {
+    double s = 0;
+    for (int rr = 0; rr < GLM_RB; ++rr) s += lps[rr * GLM_CT + t];
+    int c = c0 + t;
+    if (c < G.C) {
+      G.part_lp[(size_t)split * G.C + c] = s;
+      G.part_g[((size_t)split * G.C + c) * (K + 1)] = (double)g0acc;
+    }
+  }
+  if (t < GLM_KC) {
+    for (int kc = 0; kc < nkc; ++kc) {
+      int k = kc * GLM_KC + t;
+      if (k >= K) continue;
+      for (int cc = 0; cc < GLM_CT; ++cc) {
+        int c = c0 + cc;
+        if (c < G.C) G.part_g[((size_t)split * G.C + c) * (K + 1) + 1 + k] = (double)gacc[kc][cc];
+      }
+    }
+  }
+}
+
+}  // namespace gnuts

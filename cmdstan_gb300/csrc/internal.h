@@ -1,0 +1,71 @@
+// Internal declarations shared by the C-ABI layer (abi.cpp) and the CUDA
+// translation units.  Not part of the public interface.
+#pragma once
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "../../include/gnuts.h"
+
+namespace gnuts {
+
+enum ModelKind : int {
+  MK_BERNOULLI = 0,
+  MK_NORMAL = 1,
+  MK_LOGISTIC = 2,
+  MK_HIER = 3,
+  MK_FUNNEL = 4,
+  MK_VARINT = 5,
+  MK_HORSESHOE = 6,
+};
+
+// Device-resident model data.  Plain struct copied by value into kernels.
+struct DevModel {
+  int kind;
+  int D;       // unconstrained dimension
+  int ncon;    // write_array columns
+  int N, J, K; // sizes (meaning depends on kind)
+  int ysum;    // bernoulli: sum(y)
+  const int* yi;
+  const double* yr;
+  const double* X;       // FP64 row-major N x (D or K)
+  const float* Xf;       // FP32 copy (same values)
+  const uint16_t* Xb;    // BF16 copy (same values when X is bf16-representable)
+  const int* group;      // varint: 1-based group ids, rows sorted by group
+  const int* gstart;     // varint: J+1 row offsets
+  const double* sigma;
+  const double* scales;
+  double scale_global, slab_scale, slab_df;
+};
+
+struct Model {
+  std::string id, name;
+  DevModel dev{};
+  bool x_bf16_exact = false;
+  std::vector<std::string> con_names, unc_names;
+  // host copies used for unconstraining / write_array on the host
+  std::vector<double> host_X;
+  std::vector<int> host_yi;
+  std::vector<void*> device_allocs;
+  int device = -1;
+  ~Model();
+};
+
+struct RunConfig {
+  int metric;   // 0 diag, 1 dense, 2 unit
+  int adapt;
+};
+
+// sampler.cu
+int run_nuts(Model& m, const gnuts_sample_args& a, const RunConfig& rc, const double* inits,
+             const double* inv_metric, gnuts_output* out, gnuts_progress_fn progress, void* ctx,
+             std::string& err);
+int run_transition(Model& m, int metric, const double* inv_metric, int n, const double* q0,
+                   const double* p0, double eps, int max_depth, unsigned seed,
+                   const unsigned* chain_ids, uint64_t* counters, double* q_out, double* stats,
+                   std::string& err);
+int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, double* lp, double* grad,
+                      std::string& err);
+int run_write_array(Model& m, int n, const double* q, double* out, std::string& err);
+int upload(Model& m, std::string& err);
+
+}  // namespace gnuts

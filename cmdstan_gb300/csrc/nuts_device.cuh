@@ -1,0 +1,649 @@
+// Per-chain NUTS state machine on the device.
+//
+// Replaces stan::mcmc::base_nuts::transition / build_tree, expl_leapfrog,
+// the diag_e / dense_e / unit_e metrics, stepsize_adaptation and the
+// windowed var / covar adaptation that the hmc_nuts_* services run
+// (called from src/cmdstan/command.hpp:609-632 and 657-688).
+//
+// The recursion of build_tree becomes an explicit stack: a doubling of depth
+// d visits leaves k = 0 .. 2^d-1 in order; after leaf k the pending left
+// subtrees at heights h with bit h of k set are merged bottom-up (post-order,
+// as the recursion does), otherwise the current subtree is parked at its
+// height.  Subtree summaries live in a per-chain pool of records
+// {p_beg, p#_beg, p_end, p#_end, rho, proposal q, proposal grad} addressed by
+// index, so merges and pushes move indices, not vectors.
+//
+// One warp advances one chain; lane l owns vector elements l, l+32, ...
+// Every lane carries the same scalar state (lane-uniform control flow).
+// advance() runs the machine until the chain needs the gradient at W.q (it
+// returns true) or the chain is finished (false).  The gradient is written
+// into W.g / W_lp by the caller: inline (fused kernel) or by a batched
+// gradient kernel (round mode).
+#pragma once
+#include "device_models.cuh"
+#include "philox.cuh"
+
+namespace gnuts {
+
+enum Phase : int { PH_INIT = 0, PH_IS_FIRST = 1, PH_IS_LOOP = 2, PH_LEAF = 3, PH_DONE = 4, PH_ERROR = 5 };
+enum ChainErr : int { CE_OK = 0, CE_INIT = 1, CE_IMPROPER = 2, CE_NO_STEPSIZE = 3, CE_METRIC = 4, CE_NOT_PD = 5 };
+
+constexpr int MAXREC = 18;  // max_depth <= 16
+
+struct Scal {
+  int phase, err, iter, row;
+  int depth, n_leapfrog, divergent, dir;
+  int leaf, cur;
+  unsigned free_mask;
+  int is_dir, is_ctx, init_attempts, adapt_done, pad0;
+  double nom_eps, eps, H0, lsw, sum_metro;
+  double W_lp, F_lp, B_lp, S_lp, S_h;
+  double is_H0;
+  double da_mu, da_counter, da_sbar, da_xbar;
+  unsigned w_nw, w_ib, w_tb, w_bw, w_counter, w_size, w_next, pad1;
+  double wf_n;
+  unsigned long long rng_n, irng_n;
+  long long n_grad;
+  unsigned long long t_start, t_warm, t_end;
+  signed char stack[MAXREC];
+  double r_lsw[MAXREC], r_lp[MAXREC], r_h[MAXREC];
+};
+
+struct Params {
+  int C, D, ld, ncon, ncol, R;
+  int metric, adapt;
+  int num_warmup, num_samples, thin, save_warmup;
+  double stepsize, jitter;
+  int max_depth;
+  double delta, gamma, kappa, t0;
+  unsigned init_buffer, term_buffer, window;
+  unsigned seed, id_base;
+  double init_radius;
+  int has_init, replay, n_saved, grad_budget;
+};
+
+struct Bufs {
+  double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg;
+  double *Tpb, *Tsb, *Tpe, *Tse, *Trho;
+  double* rec;   // [C][R][7][ld]
+  double* minv;  // diag/unit [C][ld]; dense [C][D][ld]
+  double* chol;  // dense: transposed Cholesky factor Lt[k][i] = L[i][k], [C][D][ld]
+  double *wm, *wm2, *tmp;
+  double* draws;       // [C][n_saved][ncol]
+  double* out_eps;     // [C]
+  double* out_minv;    // [C][D] or [C][D*D]
+  const double* init_q;  // [C][D] (has_init)
+  const double* p0;      // [C][D] (replay)
+  Scal* sc;
+  int* done_count;
+};
+
+// record vector slots
+enum { RV_PB = 0, RV_SB = 1, RV_PE = 2, RV_SE = 3, RV_RHO = 4, RV_Q = 5, RV_G = 6 };
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ double lse(double a, double b) {
+  const double NEG_INF = -__longlong_as_double(0x7ff0000000000000ll);
+  if (a == NEG_INF) return b;
+  if (b == NEG_INF) return a;
+  double m = a > b ? a : b;
+  return m + log1p(exp(-fabs(a - b)));
+}
+
+struct Chain {
+  const Params& P;
+  const Bufs& B;
+  const DevModel& M;
+  Scal& s;
+  int c, lane, D;
+  uint32_t chain_id;
+  double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg, *Tpb, *Tsb, *Tpe, *Tse, *Trho;
+  double *minv, *chol, *wm, *wm2, *tmp;
+
+  __device__ Chain(const Params& p, const Bufs& b, const DevModel& m, Scal& sc, int ci, int ln)
+      : P(p), B(b), M(m), s(sc), c(ci), lane(ln), D(p.D) {
+    chain_id = p.id_base + (uint32_t)ci;
+    size_t o = (size_t)ci * p.ld;
+    Wq = b.Wq + o; Wp = b.Wp + o; Wg = b.Wg + o;
+    Fq = b.Fq + o; Fp = b.Fp + o; Fg = b.Fg + o;
+    Bq = b.Bq + o; Bp = b.Bp + o; Bg = b.Bg + o;
+    Sq = b.Sq + o; Sg = b.Sg + o;
+    Tpb = b.Tpb + o; Tsb = b.Tsb + o; Tpe = b.Tpe + o; Tse = b.Tse + o; Trho = b.Trho + o;
+    tmp = b.tmp + o;
+    size_t mo = p.metric == 1 ? (size_t)ci * p.D * p.ld : o;
+    minv = b.minv + mo;
+    chol = p.metric == 1 ? b.chol + mo : nullptr;
+    wm = b.wm + o;
+    wm2 = b.wm2 + mo;
+  }
+  __device__ double* rec(int r, int v) const {
+    return B.rec + (((size_t)c * P.R + r) * 7 + v) * P.ld;
+  }
+
+  // ---------------- vector helpers ----------------
+  __device__ void copy(double* dst, const double* src) const {
+    for (int d = lane; d < D; d += 32) dst[d] = src[d];
+  }
+  __device__ double dot(const double* a, const double* b) const {
+    double t = 0;
+    for (int d = lane; d < D; d += 32) t += a[d] * b[d];
+    return wsum(t);
+  }
+  // out = minv * p  (p must be visible to the whole warp for dense)
+  __device__ void dtau(double* out, const double* p) const {
+    if (P.metric == 0) {
+      for (int d = lane; d < D; d += 32) out[d] = minv[d] * p[d];
+    } else if (P.metric == 2) {
+      for (int d = lane; d < D; d += 32) out[d] = p[d];
+    } else {
+      __syncwarp();
+      for (int d = lane; d < D; d += 32) {
+        double t = 0;
+        for (int j = 0; j < D; ++j) t += minv[(size_t)j * P.ld + d] * p[j];
+        out[d] = t;
+      }
+    }
+  }
+  // kinetic energy 0.5 p.(minv p), using a precomputed ps = minv p
+  __device__ double kinetic(const double* p, const double* ps) const { return 0.5 * dot(p, ps); }
+
+  __device__ void sample_p(double* p) {
+    const uint64_t n0 = s.rng_n;
+    if (P.metric == 1) {
+      for (int d = lane; d < D; d += 32) tmp[d] = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
+      __syncwarp();
+      // solve Lt p = z, back substitution over rows of Lt (Lt[i][k] = L[k][i])
+      for (int i = D - 1; i >= 0; --i) {
+        const double* row = chol + (size_t)i * P.ld;
+        double t = 0;
+        for (int k = i + 1 + lane; k < D; k += 32) t += row[k] * p[k];
+        t = wsum(t);
+        double v = (tmp[i] - t) / row[i];
+        if (lane == (i & 31)) p[i] = v;
+        __syncwarp();
+      }
+    } else {
+      for (int d = lane; d < D; d += 32) {
+        double z = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
+        p[d] = P.metric == 0 ? z / sqrt(minv[d]) : z;
+      }
+    }
+    s.rng_n = n0 + (uint64_t)((D + 1) / 2);
+    __syncwarp();
+  }
+  __device__ double uniform() { return rng_uniform(P.seed, chain_id, 0u, s.rng_n++); }
+
+  // W.p += e/2 g ; W.q += e * minv W.p   (gradient at W.q then requested)
+  __device__ void begin_leapfrog(double e) {
+    for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
+    if (P.metric == 1) {
+      dtau(tmp, Wp);
+      for (int d = lane; d < D; d += 32) Wq[d] += e * tmp[d];
+    } else {
+      for (int d = lane; d < D; d += 32) Wq[d] += e * (P.metric == 0 ? minv[d] * Wp[d] : Wp[d]);
+    }
+    __syncwarp();
+  }
+  __device__ void complete_leapfrog(double e) {
+    for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
+    ++s.n_grad;
+    __syncwarp();
+  }
+  __device__ double energy_W(double* ps) {
+    dtau(ps, Wp);
+    return kinetic(Wp, ps) - s.W_lp;
+  }
+  __device__ void load_W_from(const double* q, const double* p, const double* g, double lp) {
+    copy(Wq, q);
+    if (p) copy(Wp, p);
+    copy(Wg, g);
+    s.W_lp = lp;
+    __syncwarp();
+  }
+
+  // ---------------- error / completion ----------------
+  __device__ void fail(int code) {
+    s.err = code;
+    s.phase = PH_ERROR;
+    s.t_end = globaltimer();
+    if (lane == 0) atomicAdd(B.done_count, 1);
+  }
+  __device__ void finish() {
+    s.phase = PH_DONE;
+    s.t_end = globaltimer();
+    if (lane == 0) atomicAdd(B.done_count, 1);
+  }
+
+  // ---------------- initialisation ----------------
+  // draws a candidate into W.q (stream 1), gradient then requested
+  __device__ void init_candidate() {
+    if (P.has_init) {
+      for (int d = lane; d < D; d += 32) Wq[d] = B.init_q[(size_t)c * D + d];
+    } else {
+      const uint64_t n0 = s.irng_n;
+      for (int d = lane; d < D; d += 32)
+        Wq[d] = P.init_radius * (2.0 * rng_uniform(P.seed, chain_id, 1u, n0 + (uint64_t)d) - 1.0);
+      s.irng_n = n0 + (uint64_t)D;
+    }
+    ++s.init_attempts;
+    s.phase = PH_INIT;
+    __syncwarp();
+  }
+  __device__ bool W_finite() const {
+    bool ok = isfinite(s.W_lp);
+    for (int d = lane; d < D; d += 32) ok = ok && isfinite(Wg[d]);
+    return wall(ok);
+  }
+
+  // ---------------- step-size search ----------------
+  // returns true if a gradient is requested
+  __device__ bool begin_init_stepsize(int ctx) {
+    s.is_ctx = ctx;
+    if (s.nom_eps == 0 || s.nom_eps > 1e7 || isnan(s.nom_eps)) return after_init_stepsize();
+    load_W_from(Sq, nullptr, Sg, s.S_lp);
+    sample_p(Wp);
+    s.is_H0 = energy_W(tmp);
+    begin_leapfrog(s.nom_eps);
+    s.phase = PH_IS_FIRST;
+    return true;
+  }
+  __device__ bool after_init_stepsize() {
+    if (s.is_ctx == 1) {
+      s.da_mu = log(10.0 * s.nom_eps);
+      s.da_counter = 0; s.da_sbar = 0; s.da_xbar = 0;
+    }
+    return begin_transition();
+  }
+  __device__ bool step_init_stepsize() {
+    complete_leapfrog(s.nom_eps);
+    double h = energy_W(tmp);
+    if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
+    double dH = s.is_H0 - h;
+    const double l08 = -0.22314355131420976;  // log(0.8)
+    if (s.phase == PH_IS_FIRST) {
+      s.is_dir = dH > l08 ? 1 : -1;
+    } else {
+      if (s.is_dir == 1 && !(dH > l08)) return after_init_stepsize();
+      if (s.is_dir == -1 && !(dH < l08)) return after_init_stepsize();
+      s.nom_eps = s.is_dir == 1 ? 2.0 * s.nom_eps : 0.5 * s.nom_eps;
+      if (s.nom_eps > 1e7) { fail(CE_IMPROPER); return false; }
+      if (s.nom_eps == 0) { fail(CE_NO_STEPSIZE); return false; }
+    }
+    load_W_from(Sq, nullptr, Sg, s.S_lp);
+    sample_p(Wp);
+    s.is_H0 = energy_W(tmp);
+    begin_leapfrog(s.nom_eps);
+    s.phase = PH_IS_LOOP;
+    return true;
+  }
+
+  // ---------------- transition ----------------
+  __device__ int alloc_rec() {
+    int r = __ffs(s.free_mask) - 1;
+    s.free_mask &= ~(1u << r);
+    return r;
+  }
+  __device__ void free_rec(int r) { s.free_mask |= (1u << r); }
+
+  __device__ bool begin_transition() {
+    const int total = P.num_warmup + P.num_samples;
+    if (s.iter >= total) { finish(); return false; }
+    if (s.iter == P.num_warmup && !s.adapt_done) {
+      s.adapt_done = 1;
+      if (P.adapt) s.nom_eps = exp(s.da_xbar);  // complete_adaptation
+      s.t_warm = globaltimer();
+      if (lane == 0) B.out_eps[c] = s.nom_eps;
+      const size_t msz = P.metric == 1 ? (size_t)D * D : (size_t)D;
+      if (P.metric == 1) {
+        for (int i = 0; i < D; ++i)
+          for (int j = lane; j < D; j += 32) B.out_minv[(size_t)c * msz + (size_t)i * D + j] = minv[(size_t)i * P.ld + j];
+      } else {
+        for (int d = lane; d < D; d += 32) B.out_minv[(size_t)c * msz + d] = minv[d];
+      }
+    }
+    s.eps = s.nom_eps;
+    if (P.jitter > 0 && !P.replay) s.eps *= 1.0 + P.jitter * (2.0 * uniform() - 1.0);
+    load_W_from(Sq, nullptr, Sg, s.S_lp);
+    if (P.replay) {
+      for (int d = lane; d < D; d += 32) Wp[d] = B.p0[(size_t)c * D + d];
+      __syncwarp();
+    } else {
+      sample_p(Wp);
+    }
+    dtau(Tsb, Wp);
+    s.H0 = kinetic(Wp, Tsb) - s.W_lp;
+    s.S_h = s.H0;
+    for (int d = lane; d < D; d += 32) {
+      double p = Wp[d];
+      Fq[d] = Wq[d]; Fp[d] = p; Fg[d] = Wg[d];
+      Bq[d] = Wq[d]; Bp[d] = p; Bg[d] = Wg[d];
+      Tpb[d] = p; Tpe[d] = p; Tse[d] = Tsb[d]; Trho[d] = p;
+    }
+    s.F_lp = s.W_lp;
+    s.B_lp = s.W_lp;
+    s.lsw = 0;
+    s.n_leapfrog = 0;
+    s.sum_metro = 0;
+    s.depth = 0;
+    s.divergent = 0;
+    __syncwarp();
+    return begin_doubling();
+  }
+
+  __device__ bool begin_doubling() {
+    s.dir = uniform() > 0.5 ? 1 : -1;
+    if (s.dir > 0) load_W_from(Fq, Fp, Fg, s.F_lp);
+    else load_W_from(Bq, Bp, Bg, s.B_lp);
+    s.leaf = 0;
+    s.free_mask = (1u << P.R) - 1u;
+    for (int h = 0; h < MAXREC; ++h) s.stack[h] = -1;
+    begin_leapfrog(s.dir * s.eps);
+    s.phase = PH_LEAF;
+    return true;
+  }
+
+  // merge pending left subtree A (init) with the current subtree Bk (final);
+  // result is left in A.  Returns the no-U-turn verdict.
+  __device__ bool merge(int A, int Bk) {
+    double lsw_sub = lse(s.r_lsw[A], s.r_lsw[Bk]);
+    bool take;
+    if (s.r_lsw[Bk] > lsw_sub) {
+      take = true;
+    } else {
+      double a = exp(s.r_lsw[Bk] - lsw_sub);
+      take = uniform() < a;
+    }
+    double *Apb = rec(A, RV_PB), *Asb = rec(A, RV_SB), *Ape = rec(A, RV_PE), *Ase = rec(A, RV_SE),
+           *Arho = rec(A, RV_RHO), *Aq = rec(A, RV_Q), *Ag = rec(A, RV_G);
+    double *Bpb = rec(Bk, RV_PB), *Bsb = rec(Bk, RV_SB), *Bpe = rec(Bk, RV_PE), *Bse = rec(Bk, RV_SE),
+           *Brho = rec(Bk, RV_RHO), *Bq_ = rec(Bk, RV_Q), *Bg_ = rec(Bk, RV_G);
+    double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;
+    for (int d = lane; d < D; d += 32) {
+      double rs = Arho[d] + Brho[d];
+      double e1 = Arho[d] + Bpb[d];
+      double e2 = Brho[d] + Ape[d];
+      s1a += Asb[d] * rs;
+      s1b += Bse[d] * rs;
+      s2a += Asb[d] * e1;
+      s2b += Bsb[d] * e1;
+      s3a += Ase[d] * e2;
+      s3b += Bse[d] * e2;
+      Arho[d] = rs;
+      Ape[d] = Bpe[d];
+      Ase[d] = Bse[d];
+      if (take) { Aq[d] = Bq_[d]; Ag[d] = Bg_[d]; }
+    }
+    s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
+    if (take) { s.r_lp[A] = s.r_lp[Bk]; s.r_h[A] = s.r_h[Bk]; }
+    s.r_lsw[A] = lsw_sub;
+    __syncwarp();
+    return (s1b > 0 && s1a > 0) && (s2b > 0 && s2a > 0) && (s3b > 0 && s3a > 0);
+  }
+
+  __device__ bool step_leaf() {
+    const double e = s.dir * s.eps;
+    complete_leapfrog(e);
+    ++s.n_leapfrog;
+    int r = alloc_rec();
+    double *pb = rec(r, RV_PB), *sb = rec(r, RV_SB), *pe = rec(r, RV_PE), *se = rec(r, RV_SE),
+           *rho = rec(r, RV_RHO), *rq = rec(r, RV_Q), *rg = rec(r, RV_G);
+    dtau(sb, Wp);
+    double h = kinetic(Wp, sb) - s.W_lp;
+    if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
+    if (h - s.H0 > 1000.0) s.divergent = 1;
+    s.sum_metro += (s.H0 - h > 0) ? 1.0 : exp(s.H0 - h);
+    for (int d = lane; d < D; d += 32) {
+      double p = Wp[d];
+      pb[d] = p; pe[d] = p; se[d] = sb[d]; rho[d] = p;
+      rq[d] = Wq[d]; rg[d] = Wg[d];
+    }
+    s.r_lsw[r] = s.H0 - h;
+    s.r_lp[r] = s.W_lp;
+    s.r_h[r] = h;
+    __syncwarp();
+    if (s.divergent) return end_transition();
+    int cur = r, height = 0;
+    while ((s.leaf >> height) & 1) {
+      int A = s.stack[height];
+      s.stack[height] = -1;
+      bool ok = merge(A, cur);
+      free_rec(cur);
+      cur = A;
+      ++height;
+      if (!ok) return end_transition();
+    }
+    if (height == s.depth) return finish_doubling(cur);
+    s.stack[height] = (signed char)cur;
+    ++s.leaf;
+    begin_leapfrog(e);
+    return true;
+  }
+
+  __device__ bool finish_doubling(int N) {
+    if (s.dir > 0) {
+      copy(Fq, Wq); copy(Fp, Wp); copy(Fg, Wg); s.F_lp = s.W_lp;
+    } else {
+      copy(Bq, Wq); copy(Bp, Wp); copy(Bg, Wg); s.B_lp = s.W_lp;
+    }
+    ++s.depth;
+    bool take;
+    if (s.r_lsw[N] > s.lsw) {
+      take = true;
+    } else {
+      double a = exp(s.r_lsw[N] - s.lsw);
+      take = uniform() < a;
+    }
+    double *Npb = rec(N, RV_PB), *Nsb = rec(N, RV_SB), *Npe = rec(N, RV_PE), *Nse = rec(N, RV_SE),
+           *Nrho = rec(N, RV_RHO), *Nq = rec(N, RV_Q), *Ng = rec(N, RV_G);
+    if (take) {
+      copy(Sq, Nq);
+      copy(Sg, Ng);
+      s.S_lp = s.r_lp[N];
+      s.S_h = s.r_h[N];
+    }
+    s.lsw = lse(s.lsw, s.r_lsw[N]);
+    // In time order the trajectory is [init | final]: forward -> (T, N),
+    // backward -> (N reversed, T).
+    double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;
+    if (s.dir > 0) {
+      for (int d = lane; d < D; d += 32) {
+        double rs = Trho[d] + Nrho[d];
+        double e1 = Trho[d] + Npb[d];
+        double e2 = Nrho[d] + Tpe[d];
+        s1a += Tsb[d] * rs; s1b += Nse[d] * rs;
+        s2a += Tsb[d] * e1; s2b += Nsb[d] * e1;
+        s3a += Tse[d] * e2; s3b += Nse[d] * e2;
+        Trho[d] = rs; Tpe[d] = Npe[d]; Tse[d] = Nse[d];
+      }
+    } else {
+      for (int d = lane; d < D; d += 32) {
+        double rs = Nrho[d] + Trho[d];
+        double e1 = Nrho[d] + Tpb[d];
+        double e2 = Trho[d] + Npb[d];
+        s1a += Nse[d] * rs; s1b += Tse[d] * rs;
+        s2a += Nse[d] * e1; s2b += Tsb[d] * e1;
+        s3a += Nsb[d] * e2; s3b += Tse[d] * e2;
+        Trho[d] = rs; Tpb[d] = Npe[d]; Tsb[d] = Nse[d];
+      }
+    }
+    s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
+    free_rec(N);
+    __syncwarp();
+    bool persist = (s1b > 0 && s1a > 0) && (s2b > 0 && s2a > 0) && (s3b > 0 && s3a > 0);
+    if (!persist || s.depth >= P.max_depth) return end_transition();
+    return begin_doubling();
+  }
+
+  __device__ void record(double accept) {
+    const bool warm = s.iter < P.num_warmup;
+    const int m = warm ? s.iter : s.iter - P.num_warmup;
+    if ((warm && !P.save_warmup) || (m % P.thin) != 0) return;
+    double* row = B.draws + ((size_t)c * P.n_saved + s.row) * P.ncol;
+    if (lane == 0) {
+      row[0] = s.S_lp; row[1] = accept; row[2] = s.eps; row[3] = s.depth;
+      row[4] = s.n_leapfrog; row[5] = s.divergent; row[6] = s.S_h;
+    }
+    warp_write_array(M, Sq, row + 7, lane);
+    ++s.row;
+  }
+
+  // returns true if a gradient is requested
+  __device__ bool end_transition() {
+    const double accept = s.sum_metro / (double)s.n_leapfrog;
+    __syncwarp();
+    record(accept);
+    const bool warm = s.iter < P.num_warmup;
+    ++s.iter;
+    if (warm && P.adapt) {
+      // stepsize_adaptation::learn_stepsize
+      s.da_counter += 1;
+      double a = accept > 1 ? 1 : accept;
+      double eta = 1.0 / (s.da_counter + P.t0);
+      s.da_sbar = (1.0 - eta) * s.da_sbar + eta * (P.delta - a);
+      double x = s.da_mu - s.da_sbar * sqrt(s.da_counter) / P.gamma;
+      double xe = pow(s.da_counter, -P.kappa);
+      s.da_xbar = (1.0 - xe) * s.da_xbar + xe * x;
+      s.nom_eps = exp(x);
+      if (P.metric != 2) {
+        if (learn_metric()) {
+          if (s.phase == PH_ERROR) return false;
+          return begin_init_stepsize(1);
+        }
+      }
+    }
+    return begin_transition();
+  }
+
+  // windowed Welford adaptation; returns true when the metric was updated
+  __device__ bool learn_metric() {
+    const bool in_window = s.w_counter >= s.w_ib && s.w_counter < s.w_nw - s.w_tb && s.w_counter != s.w_nw;
+    if (in_window) welford_add();
+    const bool end_window = s.w_counter == s.w_next && s.w_counter != s.w_nw;
+    if (!end_window) {
+      ++s.w_counter;
+      return false;
+    }
+    // compute_next_window
+    if (s.w_next != s.w_nw - s.w_tb - 1) {
+      s.w_size *= 2;
+      s.w_next = s.w_counter + s.w_size;
+      if (s.w_next != s.w_nw - s.w_tb - 1) {
+        unsigned boundary = s.w_next + 2 * s.w_size;
+        if (boundary >= s.w_nw - s.w_tb) s.w_next = s.w_nw - s.w_tb - 1;
+      }
+    }
+    const double n = s.wf_n;
+    bool ok = true;
+    if (P.metric == 1) {
+      for (int i = 0; i < D; ++i)
+        for (int j = lane; j < D; j += 32) {
+          double v = wm2[(size_t)i * P.ld + j] / (n - 1.0);
+          v = (n / (n + 5.0)) * v + (i == j ? 1e-3 * (5.0 / (n + 5.0)) : 0.0);
+          minv[(size_t)i * P.ld + j] = v;
+          ok = ok && isfinite(v);
+        }
+    } else {
+      for (int d = lane; d < D; d += 32) {
+        double v = wm2[d] / (n - 1.0);
+        v = (n / (n + 5.0)) * v + 1e-3 * (5.0 / (n + 5.0));
+        minv[d] = v;
+        ok = ok && isfinite(v);
+      }
+    }
+    __syncwarp();
+    if (!wall(ok)) { fail(CE_METRIC); return true; }
+    if (P.metric == 1 && !cholesky()) { fail(CE_NOT_PD); return true; }
+    // restart the estimator
+    s.wf_n = 0;
+    for (int d = lane; d < D; d += 32) wm[d] = 0;
+    if (P.metric == 1) {
+      for (int i = 0; i < D; ++i)
+        for (int j = lane; j < D; j += 32) wm2[(size_t)i * P.ld + j] = 0;
+    } else {
+      for (int d = lane; d < D; d += 32) wm2[d] = 0;
+    }
+    ++s.w_counter;
+    __syncwarp();
+    return true;
+  }
+
+  __device__ void welford_add() {
+    s.wf_n += 1;
+    const double n = s.wf_n;
+    for (int d = lane; d < D; d += 32) {
+      double q = Sq[d];
+      double delta = q - wm[d];
+      wm[d] += delta / n;
+      if (P.metric == 1) tmp[d] = delta;
+      else wm2[d] += (q - wm[d]) * delta;
+    }
+    if (P.metric == 1) {
+      __syncwarp();
+      for (int i = 0; i < D; ++i) {
+        double a = Sq[i] - wm[i];
+        for (int j = lane; j < D; j += 32) wm2[(size_t)i * P.ld + j] += a * tmp[j];
+      }
+    }
+    __syncwarp();
+  }
+
+  // Lt (row k holds column k of L) from minv; false if not positive definite
+  __device__ bool cholesky() {
+    for (int j = 0; j < D; ++j) {
+      double* Lj = chol + (size_t)j * P.ld;  // Lt row j = L column j
+      double t = 0;
+      for (int k = 0; k < j; ++k) {
+        double l = chol[(size_t)k * P.ld + j];
+        t += l * l;
+      }
+      double sdiag = minv[(size_t)j * P.ld + j] - t;
+      if (!(sdiag > 0)) return false;
+      double dj = sqrt(sdiag);
+      for (int i = j + 1 + lane; i < D; i += 32) {
+        double u = minv[(size_t)i * P.ld + j];
+        for (int k = 0; k < j; ++k) u -= chol[(size_t)k * P.ld + i] * chol[(size_t)k * P.ld + j];
+        Lj[i] = u / dj;
+      }
+      if (lane == 0) Lj[j] = dj;
+      for (int i = lane; i < j; i += 32) Lj[i] = 0.0;
+      __syncwarp();
+    }
+    return true;
+  }
+
+  // ---------------- driver ----------------
+  __device__ __noinline__ bool advance() {
+    switch (s.phase) {
+      case PH_INIT: {
+        if (W_finite()) {
+          copy(Sq, Wq);
+          copy(Sg, Wg);
+          s.S_lp = s.W_lp;
+          ++s.n_grad;
+          __syncwarp();
+          if (P.adapt) return begin_init_stepsize(0);
+          return begin_transition();
+        }
+        ++s.n_grad;
+        const int max_attempts = (P.has_init || P.init_radius == 0) ? 1 : 100;
+        if (s.init_attempts >= max_attempts) { fail(CE_INIT); return false; }
+        init_candidate();
+        return true;
+      }
+      case PH_IS_FIRST:
+      case PH_IS_LOOP:
+        return step_init_stepsize();
+      case PH_LEAF:
+        return step_leaf();
+      default:
+        return false;
+    }
+  }
+};
+
+}  // namespace gnuts

@@ -1,0 +1,647 @@
+// Device sampler: kernels and the host driver behind the hmc_nuts_* entry
+// points of the C ABI.
+//
+// Execution modes
+//   fused : one warp per chain runs its whole sampler (state machine +
+//           inline warp gradient) for a budget of gradient evaluations per
+//           launch; used for models without a large shared design matrix.
+//   rounds: the state machine (k_advance) and a batched gradient over all
+//           chains (grad_logistic.cu) alternate; each round every live chain
+//           needs exactly one gradient, so one contraction serves all chains.
+//           Rounds are captured in CUDA graphs.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "internal.h"
+#include "nuts_device.cuh"
+#include "batched.cuh"
+
+namespace gnuts {
+
+#define GN_CUDA(call)                                                                        \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      err = std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #call;            \
+      return GNUTS_ERR_CUDA;                                                                 \
+    }                                                                                        \
+  } while (0)
+
+struct ReplayBufs {
+  const unsigned* chain_ids;
+  const unsigned long long* rng_start;
+};
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, ReplayBufs RB) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= P.C) return;
+  Scal s;
+  memset(&s, 0, sizeof(Scal));
+  Chain ch(P, B, M, s, warp, lane);
+  if (RB.chain_ids) ch.chain_id = RB.chain_ids[warp];
+  s.t_start = globaltimer();
+  s.nom_eps = P.stepsize;
+  s.eps = P.stepsize;
+  s.rng_n = RB.rng_start ? RB.rng_start[warp] : 0ull;
+  s.irng_n = 0;
+  s.da_mu = log(10.0 * P.stepsize);
+  // windowed_adaptation::set_window_params
+  {
+    unsigned nw = (unsigned)P.num_warmup;
+    if (nw < 20) {
+      s.w_nw = 0; s.w_ib = 0; s.w_tb = 0; s.w_bw = 0;
+    } else if (P.init_buffer + P.window + P.term_buffer > nw) {
+      s.w_nw = nw;
+      s.w_ib = (unsigned)(0.15 * nw);
+      s.w_tb = (unsigned)(0.1 * nw);
+      s.w_bw = nw - (s.w_ib + s.w_tb);
+    } else {
+      s.w_nw = nw; s.w_ib = P.init_buffer; s.w_tb = P.term_buffer; s.w_bw = P.window;
+    }
+    s.w_counter = 0;
+    s.w_size = s.w_bw;
+    s.w_next = s.w_ib + s.w_size - 1;
+  }
+  const int D = P.D;
+  if (P.metric == 1) {
+    for (int i = 0; i < D; ++i)
+      for (int j = lane; j < D; j += 32) {
+        double v = inv_metric ? inv_metric[((size_t)warp * D + i) * D + j] : (i == j ? 1.0 : 0.0);
+        ch.minv[(size_t)i * P.ld + j] = v;
+        ch.wm2[(size_t)i * P.ld + j] = 0.0;
+      }
+    __syncwarp();
+    if (!ch.cholesky()) {
+      s.err = CE_NOT_PD;
+      s.phase = PH_ERROR;
+      if (lane == 0) atomicAdd(B.done_count, 1);
+      if (lane == 0) B.sc[warp] = s;
+      return;
+    }
+  } else {
+    for (int d = lane; d < D; d += 32) {
+      ch.minv[d] = (P.metric == 0 && inv_metric) ? inv_metric[(size_t)warp * D + d] : 1.0;
+      ch.wm2[d] = 0.0;
+    }
+  }
+  for (int d = lane; d < D; d += 32) {
+    ch.wm[d] = 0.0;
+    ch.Wp[d] = 0.0;
+    ch.Wg[d] = 0.0;
+  }
+  ch.init_candidate();
+  if (lane == 0) B.sc[warp] = s;
+}
+
+// Fused mode: the warp evaluates the gradient itself.
+__global__ void __launch_bounds__(128) k_fused(Params P, Bufs B, DevModel M, ReplayBufs RB) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= P.C) return;
+  Scal s = B.sc[warp];
+  if (s.phase >= PH_DONE) return;
+  Chain ch(P, B, M, s, warp, lane);
+  if (RB.chain_ids) ch.chain_id = RB.chain_ids[warp];
+  for (int b = 0; b < P.grad_budget; ++b) {
+    double lp = warp_log_prob_grad(M, ch.Wq, ch.Wg, 1, lane);
+    __syncwarp();
+    s.W_lp = lp;
+    if (!ch.advance()) break;
+  }
+  __syncwarp();
+  if (lane == 0) B.sc[warp] = s;
+}
+
+// Round mode: advance every live chain by one gradient.
+__global__ void __launch_bounds__(128) k_advance(Params P, Bufs B, DevModel M, GradOut G) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= P.C) return;
+  Scal s = B.sc[warp];
+  if (s.phase >= PH_DONE) return;
+  Chain ch(P, B, M, s, warp, lane);
+  // gather this chain's gradient from the batched kernel's partial sums
+  s.W_lp = reduce_gradient(G, M, warp, ch.Wq, ch.Wg, lane);
+  __syncwarp();
+  bool more = ch.advance();
+  if (more) stage_request(G, M, warp, ch.Wq, lane);
+  __syncwarp();
+  if (lane == 0) B.sc[warp] = s;
+}
+
+__global__ void k_log_prob_grad(DevModel M, int n, const double* q, int jac, double* lp, double* g) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  double v = warp_log_prob_grad(M, q + (size_t)warp * M.D, g + (size_t)warp * M.D, jac, lane);
+  if (lane == 0) lp[warp] = v;
+}
+
+__global__ void k_write_array(DevModel M, int n, const double* q, double* out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  warp_write_array(M, q + (size_t)warp * M.D, out + (size_t)warp * M.ncon, lane);
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+
+struct Arena {
+  std::vector<void*> ptrs;
+  ~Arena() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <class T>
+  cudaError_t alloc(T** p, size_t count) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) {
+      ptrs.push_back(v);
+      cudaMemset(v, 0, std::max<size_t>(count, 1) * sizeof(T));
+    }
+    *p = (T*)v;
+    return e;
+  }
+};
+
+const char* chain_error_message(int code) {
+  switch (code) {
+    case CE_INIT: return "Initialization failed: log density or gradient not finite at every attempted initial value";
+    case CE_IMPROPER: return "Posterior is improper. Please check your model.";
+    case CE_NO_STEPSIZE: return "No acceptably small step size could be found. Perhaps the posterior is not continuous?";
+    case CE_METRIC: return "Numerical overflow in metric adaptation. This occurs when the sampler encounters extreme values on the unconstrained space; this may happen when the posterior density function is too wide or improper. There may be problems with your model specification.";
+    case CE_NOT_PD: return "Inverse metric is not positive definite";
+  }
+  return "unknown sampler error";
+}
+
+int ensure_device(std::string& err) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    err = "no CUDA device available (the sampler runs on the GPU only)";
+    return GNUTS_ERR_CUDA;
+  }
+  return GNUTS_OK;
+}
+
+bool use_rounds(const Model& m) {
+  return batched_supported(m.dev) && m.dev.N >= 4096;
+}
+
+}  // namespace
+
+int upload(Model& m, std::string& err) {
+  if (m.device >= 0) return GNUTS_OK;
+  int rc = ensure_device(err);
+  if (rc) return rc;
+  auto put = [&](const void* src, size_t bytes, void** dst) -> int {
+    if (bytes == 0) { *dst = nullptr; return GNUTS_OK; }
+    cudaError_t e = cudaMalloc(dst, bytes);
+    if (e != cudaSuccess) { err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
+    m.device_allocs.push_back(*dst);
+    e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { err = std::string("cudaMemcpy: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
+    return GNUTS_OK;
+  };
+  // The host-side Model holds host pointers in dev.*; replace them by device copies.
+  DevModel h = m.dev;
+  DevModel d = h;
+  size_t xcols = (h.kind == MK_VARINT) ? (size_t)h.K : (size_t)h.K;
+  size_t xn = (size_t)h.N * xcols;
+  if (h.yi && (rc = put(h.yi, sizeof(int) * h.N, (void**)&d.yi))) return rc;
+  if (h.yr) {
+    size_t n = h.kind == MK_HIER ? (size_t)h.J : (size_t)h.N;
+    if ((rc = put(h.yr, sizeof(double) * n, (void**)&d.yr))) return rc;
+  }
+  if (h.X && xn) {
+    if ((rc = put(h.X, sizeof(double) * xn, (void**)&d.X))) return rc;
+    std::vector<float> xf(xn);
+    std::vector<uint16_t> xb(xn);
+    for (size_t i = 0; i < xn; ++i) {
+      float f = (float)h.X[i];
+      xf[i] = f;
+      uint32_t u;
+      std::memcpy(&u, &f, 4);
+      uint32_t r = u + 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
+      xb[i] = (uint16_t)(r >> 16);
+    }
+    if ((rc = put(xf.data(), sizeof(float) * xn, (void**)&d.Xf))) return rc;
+    if ((rc = put(xb.data(), sizeof(uint16_t) * xn, (void**)&d.Xb))) return rc;
+  }
+  if (h.group && (rc = put(h.group, sizeof(int) * h.N, (void**)&d.group))) return rc;
+  if (h.gstart && (rc = put(h.gstart, sizeof(int) * (h.J + 1), (void**)&d.gstart))) return rc;
+  if (h.sigma && (rc = put(h.sigma, sizeof(double) * h.J, (void**)&d.sigma))) return rc;
+  if (h.scales && (rc = put(h.scales, sizeof(double) * h.K, (void**)&d.scales))) return rc;
+  m.dev = d;
+  cudaGetDevice(&m.device);
+  return GNUTS_OK;
+}
+
+
+// ---------------------------------------------------------------- round mode
+__global__ void k_stage(GradOut G, Params P, Bufs B, DevModel M) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= P.C) return;
+  if (B.sc[warp].phase >= PH_DONE) return;
+  stage_request(G, M, warp, B.Wq + (size_t)warp * P.ld, lane);
+}
+
+__global__ void k_stage_points(GradOut G, DevModel M, int n, const double* q) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  stage_request(G, M, warp, q + (size_t)warp * M.D, lane);
+}
+
+__global__ void k_reduce_points(GradOut G, DevModel M, int n, const double* q, int jac, double* lp, double* g) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  double v = reduce_gradient(G, M, warp, q + (size_t)warp * M.D, g + (size_t)warp * M.D, lane);
+  if (!jac && M.kind == MK_HORSESHOE) {
+    // remove the Jacobian terms added by reduce_gradient
+    const int K = M.K;
+    const double* qq = q + (size_t)warp * M.D;
+    double* gg = g + (size_t)warp * M.D;
+    double jl = 0;
+    for (int d = lane; d < K; d += 32) { jl += qq[K + 2 + d]; gg[K + 2 + d] -= 1.0; }
+    jl = wsum(jl);
+    v -= jl + qq[K + 1] + qq[2 * K + 2];
+    __syncwarp();
+    if (lane == 0) { gg[K + 1] -= 1.0; gg[2 * K + 2] -= 1.0; }
+  }
+  if (lane == 0) lp[warp] = v;
+}
+
+namespace {
+
+struct GradSetup {
+  Arena ar;
+  GradOut G{};
+};
+
+int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* done_count, std::string& err) {
+  GradOut& G = gs.G;
+  G.kind = M.kind;
+  G.prec = prec;
+  G.C = C;
+  G.C_total = C;
+  G.K = M.K;
+  // row splits: enough CTAs to fill 152 SMs a few times over
+  const int ctiles = (C + GLM_CT - 1) / GLM_CT;
+  int S = std::max(1, (152 * 4 + ctiles - 1) / ctiles);
+  S = std::min(S, std::max(1, M.N / 256));
+  G.S = S;
+  G.rows_per_split = (M.N + S - 1) / S;
+  G.rows_per_split = (G.rows_per_split + GLM_RB - 1) / GLM_RB * GLM_RB;
+  G.S = (M.N + G.rows_per_split - 1) / G.rows_per_split;
+  G.done_count = done_count;
+  GN_CUDA(gs.ar.alloc(&G.coef64, (size_t)C * (M.K + 1)));
+  GN_CUDA(gs.ar.alloc(&G.coef32, (size_t)C * (M.K + 1)));
+  GN_CUDA(gs.ar.alloc(&G.part_lp, (size_t)G.S * C));
+  GN_CUDA(gs.ar.alloc(&G.part_g, (size_t)G.S * C * (M.K + 1)));
+  return GNUTS_OK;
+}
+
+void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
+  dim3 grid((G.C + GLM_CT - 1) / GLM_CT, G.S);
+  const bool small = M.K <= GLM_KC;
+  if (G.prec == GNUTS_PRECISION_FP64) {
+    if (small) k_glm_simt<double, 1><<<grid, GLM_THREADS, 0, st>>>(G, M);
+    else k_glm_simt<double, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
+  } else {
+    if (small) k_glm_simt<float, 1><<<grid, GLM_THREADS, 0, st>>>(G, M);
+    else k_glm_simt<float, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
+  }
+}
+
+}  // namespace
+
+int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, double* dl, double* dg, int prec,
+                          std::string& err) {
+  if (M.K > 1024) { err = "batched gradient supports at most 1024 predictors"; return GNUTS_ERR_ARGUMENT; }
+  GradSetup gs;
+  int st = setup_grad(gs, M, n, prec, nullptr, err);
+  if (st) return st;
+  const int threads = 128, blocks = (n * 32 + threads - 1) / threads;
+  k_stage_points<<<blocks, threads>>>(gs.G, M, n, dq);
+  launch_glm(gs.G, M, 0);
+  k_reduce_points<<<blocks, threads>>>(gs.G, M, n, dq, jac, dl, dg);
+  GN_CUDA(cudaGetLastError());
+  GN_CUDA(cudaDeviceSynchronize());
+  return GNUTS_OK;
+}
+
+static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double per_chain_max, int refresh,
+                      gnuts_progress_fn progress, void* ctx, std::string& err) {
+  const DevModel& M = m.dev;
+  if (M.K > 1024) { err = "batched gradient supports at most 1024 predictors"; return GNUTS_ERR_ARGUMENT; }
+  GradSetup gs;
+  int st = setup_grad(gs, M, P.C, prec, B.done_count, err);
+  if (st) return st;
+  const GradOut& G = gs.G;
+  cudaStream_t stream;
+  GN_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{stream};
+  const int threads = 128, blocks = (P.C * 32 + threads - 1) / threads;
+  GN_CUDA(cudaDeviceSynchronize());  // k_init done
+  k_stage<<<blocks, threads, 0, stream>>>(G, P, B, M);
+  GN_CUDA(cudaGetLastError());
+  // capture ROUNDS x (gradient, advance) as one graph
+  const int ROUNDS = 16;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  GN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  for (int r = 0; r < ROUNDS; ++r) {
+    launch_glm(G, M, stream);
+    k_advance<<<blocks, threads, 0, stream>>>(P, B, M, G);
+  }
+  GN_CUDA(cudaStreamEndCapture(stream, &graph));
+  GN_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  struct GraphGuard { cudaGraph_t g; cudaGraphExec_t e; ~GraphGuard() { cudaGraphExecDestroy(e); cudaGraphDestroy(g); } } gg{graph, exec};
+  int* h_done = nullptr;
+  GN_CUDA(cudaMallocHost(&h_done, sizeof(int) * 2));
+  struct HostGuard { int* p; ~HostGuard() { cudaFreeHost(p); } } hg{h_done};
+  h_done[0] = h_done[1] = 0;
+  cudaEvent_t ev[2];
+  GN_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+  GN_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+  const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
+  int last_reported = -1;
+  for (long long l = 0; l < max_graphs; ++l) {
+    const int b = (int)(l & 1);
+    GN_CUDA(cudaGraphLaunch(exec, stream));
+    GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    GN_CUDA(cudaEventRecord(ev[b], stream));
+    if (l > 0) {
+      GN_CUDA(cudaEventSynchronize(ev[b ^ 1]));
+      if (h_done[b ^ 1] >= P.C) break;
+      if (progress && refresh > 0 && (l & 63) == 0) {
+        Scal s0;
+        GN_CUDA(cudaMemcpy(&s0, B.sc, sizeof(Scal), cudaMemcpyDeviceToHost));
+        if (s0.iter / refresh != last_reported) {
+          last_reported = s0.iter / refresh;
+          progress(ctx, 0, s0.iter, P.num_warmup + P.num_samples, s0.iter < P.num_warmup);
+        }
+      }
+    }
+  }
+  GN_CUDA(cudaStreamSynchronize(stream));
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  return GNUTS_OK;
+}
+
+static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& rc, const double* inits,
+                         const double* inv_metric, const double* p0, const unsigned* chain_ids,
+                         uint64_t* counters, double* replay_q_out, gnuts_output* out,
+                         gnuts_progress_fn progress, void* ctx, std::string& err);
+
+int run_nuts(Model& m, const gnuts_sample_args& a, const RunConfig& rc, const double* inits,
+             const double* inv_metric, gnuts_output* out, gnuts_progress_fn progress, void* ctx,
+             std::string& err) {
+  return run_nuts_impl(m, a, rc, inits, inv_metric, nullptr, nullptr, nullptr, nullptr, out, progress, ctx, err);
+}
+
+static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& rc, const double* inits,
+                         const double* inv_metric, const double* p0, const unsigned* chain_ids,
+                         uint64_t* counters, double* replay_q_out, gnuts_output* out,
+                         gnuts_progress_fn progress, void* ctx, std::string& err) {
+  int st = upload(m, err);
+  if (st) return st;
+  const int C = a.num_chains, D = m.dev.D;
+  Params P{};
+  P.C = C;
+  P.D = D;
+  P.ld = (D + 3) & ~3;
+  P.ncon = m.dev.ncon;
+  P.ncol = 7 + P.ncon;
+  P.max_depth = a.max_depth;
+  P.R = a.max_depth + 2;
+  P.metric = rc.metric;
+  P.adapt = rc.adapt;
+  P.num_warmup = a.num_warmup;
+  P.num_samples = a.num_samples;
+  P.thin = a.thin;
+  P.save_warmup = a.save_warmup;
+  P.stepsize = a.stepsize;
+  P.jitter = a.stepsize_jitter;
+  P.delta = a.delta;
+  P.gamma = a.gamma;
+  P.kappa = a.kappa;
+  P.t0 = a.t0;
+  P.init_buffer = a.init_buffer;
+  P.term_buffer = a.term_buffer;
+  P.window = a.window;
+  P.seed = a.seed;
+  P.id_base = a.chain_id;
+  P.init_radius = a.init_radius;
+  P.has_init = inits != nullptr;
+  P.replay = p0 != nullptr;
+  P.n_saved = (a.save_warmup ? (a.num_warmup + a.thin - 1) / a.thin : 0) + (a.num_samples + a.thin - 1) / a.thin;
+  P.grad_budget = 2048;
+
+  Arena ar;
+  Bufs B{};
+  const size_t vec = (size_t)C * P.ld;
+  const size_t mat = P.metric == 1 ? (size_t)C * D * P.ld : vec;
+  double** vecs[] = {&B.Wq, &B.Wp, &B.Wg, &B.Fq, &B.Fp, &B.Fg, &B.Bq, &B.Bp, &B.Bg, &B.Sq, &B.Sg,
+                     &B.Tpb, &B.Tsb, &B.Tpe, &B.Tse, &B.Trho, &B.wm, &B.tmp};
+  for (double** v : vecs) GN_CUDA(ar.alloc(v, vec));
+  GN_CUDA(ar.alloc(&B.rec, vec * P.R * 7));
+  GN_CUDA(ar.alloc(&B.minv, mat));
+  GN_CUDA(ar.alloc(&B.wm2, mat));
+  if (P.metric == 1) GN_CUDA(ar.alloc(&B.chol, mat));
+  GN_CUDA(ar.alloc(&B.draws, (size_t)C * P.n_saved * P.ncol));
+  GN_CUDA(ar.alloc(&B.out_eps, C));
+  const size_t msz = P.metric == 1 ? (size_t)D * D : (size_t)D;
+  GN_CUDA(ar.alloc(&B.out_minv, (size_t)C * msz));
+  GN_CUDA(ar.alloc(&B.sc, C));
+  GN_CUDA(ar.alloc(&B.done_count, 1));
+  double* d_inv = nullptr;
+  if (inv_metric) {
+    GN_CUDA(ar.alloc(&d_inv, (size_t)C * msz));
+    GN_CUDA(cudaMemcpy(d_inv, inv_metric, sizeof(double) * C * msz, cudaMemcpyHostToDevice));
+  }
+  if (inits) {
+    double* d;
+    GN_CUDA(ar.alloc(&d, (size_t)C * D));
+    GN_CUDA(cudaMemcpy(d, inits, sizeof(double) * C * D, cudaMemcpyHostToDevice));
+    B.init_q = d;
+  }
+  if (p0) {
+    double* d;
+    GN_CUDA(ar.alloc(&d, (size_t)C * D));
+    GN_CUDA(cudaMemcpy(d, p0, sizeof(double) * C * D, cudaMemcpyHostToDevice));
+    B.p0 = d;
+  }
+  ReplayBufs RB{nullptr, nullptr};
+  if (chain_ids) {
+    unsigned* d;
+    GN_CUDA(ar.alloc(&d, C));
+    GN_CUDA(cudaMemcpy(d, chain_ids, sizeof(unsigned) * C, cudaMemcpyHostToDevice));
+    RB.chain_ids = d;
+  }
+  if (counters) {
+    unsigned long long* d;
+    GN_CUDA(ar.alloc(&d, C));
+    GN_CUDA(cudaMemcpy(d, counters, sizeof(uint64_t) * C, cudaMemcpyHostToDevice));
+    RB.rng_start = d;
+  }
+
+  const int threads = 128;
+  const int blocks = (C * 32 + threads - 1) / threads;
+  k_init<<<blocks, threads>>>(P, B, m.dev, d_inv, RB);
+  GN_CUDA(cudaGetLastError());
+
+  // Upper bound on launches: every transition needs at most 2^max_depth
+  // gradients; step-size searches are bounded by the 1e7 / 0 step-size
+  // limits (about 1100 halvings or 24 doublings per search).
+  const double per_chain_max = (double)(a.num_warmup + a.num_samples) * (double)(1 << std::min(a.max_depth, 20)) +
+                               8.0 * 1200.0 + 200.0;
+  int done = 0;
+  if (use_rounds(m) && !p0) {
+    st = run_rounds(m, P, B, a.precision, per_chain_max, a.refresh, progress, ctx, err);
+    if (st) return st;
+    GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
+  } else {
+    const long long max_launches = (long long)(per_chain_max / P.grad_budget) + 16;
+    int last_reported = -1;
+    for (long long l = 0; l < max_launches; ++l) {
+      k_fused<<<blocks, threads>>>(P, B, m.dev, RB);
+      GN_CUDA(cudaGetLastError());
+      GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
+      if (progress && a.refresh > 0) {
+        Scal s0;
+        GN_CUDA(cudaMemcpy(&s0, B.sc, sizeof(Scal), cudaMemcpyDeviceToHost));
+        int it = s0.iter;
+        if (it / a.refresh != last_reported) {
+          last_reported = it / a.refresh;
+          progress(ctx, 0, it, a.num_warmup + a.num_samples, it < a.num_warmup);
+        }
+      }
+      if (done >= C) break;
+    }
+  }
+  GN_CUDA(cudaDeviceSynchronize());
+  if (done < C) {
+    err = "sampler did not finish within its launch bound";
+    return GNUTS_ERR_TIMEOUT;
+  }
+
+  std::vector<Scal> sc(C);
+  GN_CUDA(cudaMemcpy(sc.data(), B.sc, sizeof(Scal) * C, cudaMemcpyDeviceToHost));
+  if (out) {
+    if (out->draws)
+      GN_CUDA(cudaMemcpy(out->draws, B.draws, sizeof(double) * C * P.n_saved * P.ncol, cudaMemcpyDeviceToHost));
+    if (out->stepsize) GN_CUDA(cudaMemcpy(out->stepsize, B.out_eps, sizeof(double) * C, cudaMemcpyDeviceToHost));
+    if (out->inv_metric)
+      GN_CUDA(cudaMemcpy(out->inv_metric, B.out_minv, sizeof(double) * C * msz, cudaMemcpyDeviceToHost));
+    for (int c = 0; c < C; ++c) {
+      if (out->warmup_seconds) out->warmup_seconds[c] = (double)(sc[c].t_warm - sc[c].t_start) * 1e-9;
+      if (out->sampling_seconds) out->sampling_seconds[c] = (double)(sc[c].t_end - sc[c].t_warm) * 1e-9;
+      if (out->n_grad) out->n_grad[c] = sc[c].n_grad;
+      if (out->chain_status) out->chain_status[c] = sc[c].err ? (sc[c].err == CE_INIT ? GNUTS_ERR_INIT : GNUTS_ERR_SAMPLER) : GNUTS_OK;
+    }
+  }
+  if (counters)
+    for (int c = 0; c < C; ++c) counters[c] = sc[c].rng_n;
+  for (int c = 0; c < C; ++c) {
+    if (sc[c].err) {
+      char buf[64];
+      snprintf(buf, sizeof buf, "chain %u: ", (chain_ids ? chain_ids[c] : a.chain_id + c));
+      err = std::string(buf) + chain_error_message(sc[c].err);
+      return sc[c].err == CE_INIT ? GNUTS_ERR_INIT : GNUTS_ERR_SAMPLER;
+    }
+  }
+  if (replay_q_out)
+    GN_CUDA(cudaMemcpy2D(replay_q_out, sizeof(double) * D, B.Sq, sizeof(double) * P.ld, sizeof(double) * D, C,
+                         cudaMemcpyDeviceToHost));
+  return GNUTS_OK;
+}
+
+int run_transition(Model& m, int metric, const double* inv_metric, int n, const double* q0, const double* p0,
+                   double eps, int max_depth, unsigned seed, const unsigned* chain_ids, uint64_t* counters,
+                   double* q_out, double* stats, std::string& err) {
+  gnuts_sample_args a;
+  gnuts_sample_args_default(&a);
+  a.num_chains = n;
+  a.seed = seed;
+  a.num_warmup = 0;
+  a.num_samples = 1;
+  a.thin = 1;
+  a.save_warmup = 0;
+  a.stepsize = eps;
+  a.stepsize_jitter = 0;
+  a.max_depth = max_depth;
+  const int D = m.dev.D;
+  const size_t msz = metric == 1 ? (size_t)D * D : (size_t)D;
+  std::vector<double> im;
+  if (metric != 2 && inv_metric) {
+    im.resize((size_t)n * msz);
+    for (int i = 0; i < n; ++i) std::memcpy(&im[(size_t)i * msz], inv_metric, sizeof(double) * msz);
+  }
+  const int ncol = 7 + m.dev.ncon;
+  std::vector<double> draws((size_t)n * ncol);
+  gnuts_output out{};
+  out.draws = draws.data();
+  RunConfig rc{metric, 0};
+  int st = run_nuts_impl(m, a, rc, q0, im.empty() ? nullptr : im.data(), p0, chain_ids, counters, q_out, &out,
+                         nullptr, nullptr, err);
+  if (st) return st;
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 7; ++k) stats[(size_t)i * 7 + k] = draws[(size_t)i * ncol + k];
+  return GNUTS_OK;
+}
+
+int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, double* lp, double* grad, std::string& err) {
+  int st = upload(m, err);
+  if (st) return st;
+  if (n <= 0) return GNUTS_OK;
+  const int D = m.dev.D;
+  Arena ar;
+  double *dq, *dg, *dl;
+  GN_CUDA(ar.alloc(&dq, (size_t)n * D));
+  GN_CUDA(ar.alloc(&dg, (size_t)n * D));
+  GN_CUDA(ar.alloc(&dl, n));
+  GN_CUDA(cudaMemcpy(dq, q, sizeof(double) * n * D, cudaMemcpyHostToDevice));
+  if (batched_supported(m.dev) && m.dev.N >= 4096) {
+    st = batched_log_prob_grad(m.dev, n, dq, jacobian, dl, dg, GNUTS_PRECISION_FP64, err);
+    if (st) return st;
+  } else {
+    const int threads = 128, blocks = (n * 32 + threads - 1) / threads;
+    k_log_prob_grad<<<blocks, threads>>>(m.dev, n, dq, jacobian, dl, dg);
+    GN_CUDA(cudaGetLastError());
+  }
+  GN_CUDA(cudaMemcpy(lp, dl, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  GN_CUDA(cudaMemcpy(grad, dg, sizeof(double) * n * D, cudaMemcpyDeviceToHost));
+  return GNUTS_OK;
+}
+
+int run_write_array(Model& m, int n, const double* q, double* out, std::string& err) {
+  int st = upload(m, err);
+  if (st) return st;
+  if (n <= 0) return GNUTS_OK;
+  const int D = m.dev.D, K = m.dev.ncon;
+  Arena ar;
+  double *dq, *dout;
+  GN_CUDA(ar.alloc(&dq, (size_t)n * D));
+  GN_CUDA(ar.alloc(&dout, (size_t)n * K));
+  GN_CUDA(cudaMemcpy(dq, q, sizeof(double) * n * D, cudaMemcpyHostToDevice));
+  const int threads = 128, blocks = (n * 32 + threads - 1) / threads;
+  k_write_array<<<blocks, threads>>>(m.dev, n, dq, dout);
+  GN_CUDA(cudaGetLastError());
+  GN_CUDA(cudaMemcpy(out, dout, sizeof(double) * n * K, cudaMemcpyDeviceToHost));
+  return GNUTS_OK;
+}
+
+}  // namespace gnuts

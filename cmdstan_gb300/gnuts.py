@@ -1,0 +1,268 @@
+"""Python mirror of the gnuts C ABI (include/gnuts.h), through ctypes.
+
+This mirrors the reference's sampling-service interface for Python callers
+and tests: ``Model`` stands for a stanc-generated ``model_base`` built from a
+var_context (src/cmdstan/command.hpp:165-171), and ``Model.sample`` calls the
+``hmc_nuts_{diag,dense,unit}_e[_adapt]`` service that command() dispatches to
+(command.hpp:609-697), with CmdStan's argument names and defaults.
+
+The shared library is required: importing works without it, but every call
+that needs it raises ``GnutsError`` (there is no CPU fallback).
+"""
+import ctypes
+import os
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgnuts.so")
+
+GNUTS_OK = 0
+ERR_ARGUMENT, ERR_DATA, ERR_INIT, ERR_SAMPLER, ERR_CUDA, ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+VAR_INT, VAR_REAL = 0, 1
+SAMPLER_COLUMNS = ["lp__", "accept_stat__", "stepsize__", "treedepth__", "n_leapfrog__", "divergent__",
+                   "energy__"]
+METRICS = {"diag_e": 0, "dense_e": 1, "unit_e": 2}
+
+# every symbol declared in include/gnuts.h
+EXPORTS = [
+    "gnuts_model_create", "gnuts_model_create_json", "gnuts_model_destroy", "gnuts_model_dims",
+    "gnuts_model_name", "gnuts_model_param_name", "gnuts_log_prob_grad", "gnuts_unconstrain",
+    "gnuts_write_array", "gnuts_sample_args_default", "gnuts_hmc_nuts_diag_e_adapt",
+    "gnuts_hmc_nuts_dense_e_adapt", "gnuts_hmc_nuts_unit_e_adapt", "gnuts_hmc_nuts_diag_e",
+    "gnuts_hmc_nuts_dense_e", "gnuts_hmc_nuts_unit_e", "gnuts_transition", "gnuts_last_error",
+    "gnuts_version",
+]
+
+
+class GnutsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gnuts error %d: %s" % (code, msg))
+        self.code = code
+        self.msg = msg
+
+
+class SampleArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_chains", ctypes.c_int), ("chain_id", ctypes.c_uint), ("seed", ctypes.c_uint),
+        ("init_radius", ctypes.c_double), ("num_warmup", ctypes.c_int), ("num_samples", ctypes.c_int),
+        ("thin", ctypes.c_int), ("save_warmup", ctypes.c_int), ("refresh", ctypes.c_int),
+        ("stepsize", ctypes.c_double), ("stepsize_jitter", ctypes.c_double), ("max_depth", ctypes.c_int),
+        ("delta", ctypes.c_double), ("gamma", ctypes.c_double), ("kappa", ctypes.c_double),
+        ("t0", ctypes.c_double), ("init_buffer", ctypes.c_uint), ("term_buffer", ctypes.c_uint),
+        ("window", ctypes.c_uint), ("precision", ctypes.c_int),
+    ]
+
+
+class Var(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("type", ctypes.c_int), ("ndim", ctypes.c_int),
+                ("dims", ctypes.POINTER(ctypes.c_int64)), ("data", ctypes.c_void_p)]
+
+
+class Output(ctypes.Structure):
+    _fields_ = [("draws", ctypes.c_void_p), ("stepsize", ctypes.c_void_p), ("inv_metric", ctypes.c_void_p),
+                ("warmup_seconds", ctypes.c_void_p), ("sampling_seconds", ctypes.c_void_p),
+                ("n_grad", ctypes.c_void_p), ("chain_status", ctypes.c_void_p)]
+
+
+PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int)
+
+_lib = None
+
+
+def load():
+    """Load libgnuts.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GnutsError(ERR_CUDA, "libgnuts.so not built (run __graft_entry__.build())")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+    lib.gnuts_model_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(Var), ip, ctypes.c_uint,
+                                       ctypes.POINTER(vp)]
+    lib.gnuts_model_create_json.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.POINTER(vp)]
+    lib.gnuts_model_destroy.argtypes = [vp]
+    lib.gnuts_model_destroy.restype = None
+    lib.gnuts_model_dims.argtypes = [vp, ctypes.POINTER(ip), ctypes.POINTER(ip)]
+    lib.gnuts_model_name.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    lib.gnuts_model_param_name.argtypes = [vp, ip, ip, ctypes.c_char_p, ctypes.c_size_t]
+    lib.gnuts_log_prob_grad.argtypes = [vp, ip, dp, ip, dp, dp]
+    lib.gnuts_unconstrain.argtypes = [vp, dp, dp]
+    lib.gnuts_write_array.argtypes = [vp, ip, dp, dp]
+    lib.gnuts_sample_args_default.argtypes = [ctypes.POINTER(SampleArgs)]
+    lib.gnuts_sample_args_default.restype = None
+    for name in ("gnuts_hmc_nuts_diag_e_adapt", "gnuts_hmc_nuts_dense_e_adapt", "gnuts_hmc_nuts_diag_e",
+                 "gnuts_hmc_nuts_dense_e"):
+        getattr(lib, name).argtypes = [vp, ctypes.POINTER(SampleArgs), dp, dp, ctypes.POINTER(Output),
+                                       PROGRESS_FN, vp]
+    for name in ("gnuts_hmc_nuts_unit_e_adapt", "gnuts_hmc_nuts_unit_e"):
+        getattr(lib, name).argtypes = [vp, ctypes.POINTER(SampleArgs), dp, ctypes.POINTER(Output), PROGRESS_FN, vp]
+    lib.gnuts_transition.argtypes = [vp, ip, dp, ip, dp, dp, ctypes.c_double, ip, ctypes.c_uint,
+                                     ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint64), dp, dp]
+    lib.gnuts_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.gnuts_version.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+def _check(rc):
+    if rc != GNUTS_OK:
+        lib = load()
+        buf = ctypes.create_string_buffer(4096)
+        lib.gnuts_last_error(buf, len(buf))
+        raise GnutsError(rc, buf.value.decode(errors="replace"))
+
+
+def default_args(**kw):
+    a = SampleArgs()
+    load().gnuts_sample_args_default(ctypes.byref(a))
+    for k, v in kw.items():
+        if not hasattr(a, k):
+            raise TypeError("unknown sampler argument %r" % k)
+        setattr(a, k, v)
+    return a
+
+
+class Fit:
+    """Draws and adaptation results of one run (per chain)."""
+
+    def __init__(self, columns, draws, stepsize, inv_metric, warmup_seconds, sampling_seconds, n_grad, status):
+        self.columns = columns
+        self.draws = draws                    # [chains, n_saved, 7 + num_constrained]
+        self.stepsize = stepsize
+        self.inv_metric = inv_metric
+        self.warmup_seconds = warmup_seconds
+        self.sampling_seconds = sampling_seconds
+        self.n_grad = n_grad
+        self.status = status
+
+    def column(self, name):
+        return self.draws[:, :, self.columns.index(name)]
+
+
+class Model:
+    """A built-in model with its data, on the GPU (model_base equivalent)."""
+
+    def __init__(self, model_id, data=None, json_text=None, seed=0):
+        lib = load()
+        h = ctypes.c_void_p()
+        keep = []
+        if json_text is not None:
+            _check(lib.gnuts_model_create_json(model_id.encode(), json_text.encode(), seed, ctypes.byref(h)))
+        else:
+            data = data or {}
+            vars_ = (Var * max(1, len(data)))()
+            for i, (name, value) in enumerate(data.items()):
+                arr = np.asarray(value)
+                is_int = np.issubdtype(arr.dtype, np.integer) or arr.dtype == np.bool_
+                # np.array keeps 0-d scalars 0-d (ascontiguousarray would make them 1-d)
+                arr = np.array(arr, dtype=np.int32 if is_int else np.float64, order="C", copy=True)
+                dims = (ctypes.c_int64 * max(1, arr.ndim))(*arr.shape)
+                nb = name.encode()
+                keep += [arr, dims, nb]
+                vars_[i].name = nb
+                vars_[i].type = VAR_INT if is_int else VAR_REAL
+                vars_[i].ndim = arr.ndim
+                vars_[i].dims = dims
+                vars_[i].data = arr.ctypes.data_as(ctypes.c_void_p)
+            _check(lib.gnuts_model_create(model_id.encode(), vars_, len(data), seed, ctypes.byref(h)))
+        self._h = h
+        self._lib = lib
+        d, c = ctypes.c_int(), ctypes.c_int()
+        _check(lib.gnuts_model_dims(h, ctypes.byref(d), ctypes.byref(c)))
+        self.dim = d.value
+        self.num_constrained = c.value
+        buf = ctypes.create_string_buffer(256)
+        _check(lib.gnuts_model_name(h, buf, 256))
+        self.name = buf.value.decode()
+        self.param_names = []
+        for i in range(self.num_constrained):
+            _check(lib.gnuts_model_param_name(h, i, 0, buf, 256))
+            self.param_names.append(buf.value.decode())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.gnuts_model_destroy(h)
+            self._h = None
+
+    # -- model_base surface
+    def log_prob_grad(self, q, jacobian=True):
+        q = np.ascontiguousarray(np.atleast_2d(q), dtype=np.float64)
+        n = q.shape[0]
+        lp = np.zeros(n)
+        g = np.zeros((n, self.dim))
+        _check(self._lib.gnuts_log_prob_grad(self._h, n, _dp(q), int(bool(jacobian)), _dp(lp), _dp(g)))
+        return lp, g
+
+    def unconstrain(self, constrained):
+        c = np.ascontiguousarray(constrained, dtype=np.float64)
+        q = np.zeros(self.dim)
+        _check(self._lib.gnuts_unconstrain(self._h, _dp(c), _dp(q)))
+        return q
+
+    def write_array(self, q):
+        q = np.ascontiguousarray(np.atleast_2d(q), dtype=np.float64)
+        out = np.zeros((q.shape[0], self.num_constrained))
+        _check(self._lib.gnuts_write_array(self._h, q.shape[0], _dp(q), _dp(out)))
+        return out
+
+    # -- services
+    def sample(self, metric="diag_e", adapt=True, inits=None, inv_metric=None, progress=None, **kw):
+        """Run hmc_nuts_<metric>[_adapt]; keyword arguments are gnuts_sample_args fields."""
+        a = default_args(**kw)
+        C, D = a.num_chains, self.dim
+        mk = METRICS[metric]
+        th = max(1, a.thin)  # the library rejects thin < 1 itself
+        n_saved = max(0, ((a.num_warmup + th - 1) // th if a.save_warmup else 0) + (a.num_samples + th - 1) // th)
+        ncol = 7 + self.num_constrained
+        draws = np.zeros((C, n_saved, ncol))
+        eps = np.zeros(C)
+        msz = D * D if mk == 1 else D
+        minv = np.zeros((C, msz))
+        tw, ts = np.zeros(C), np.zeros(C)
+        ng = np.zeros(C, dtype=np.int64)
+        stt = np.zeros(C, dtype=np.int32)
+        out = Output(draws.ctypes.data, eps.ctypes.data, minv.ctypes.data, tw.ctypes.data, ts.ctypes.data,
+                     ng.ctypes.data, stt.ctypes.data)
+        if inits is not None:
+            inits = np.ascontiguousarray(np.broadcast_to(np.asarray(inits, dtype=np.float64), (C, D)))
+        if inv_metric is not None:
+            im = np.asarray(inv_metric, dtype=np.float64)
+            im = np.ascontiguousarray(np.broadcast_to(im.reshape(-1), (C, msz)) if im.ndim <= 2 and
+                                      im.size == msz else im.reshape(C, msz))
+        else:
+            im = None
+        cb = PROGRESS_FN(progress) if progress else PROGRESS_FN()
+        name = "gnuts_hmc_nuts_%s%s" % (metric, "_adapt" if adapt else "")
+        fn = getattr(self._lib, name)
+        if mk == 2:
+            rc = fn(self._h, ctypes.byref(a), _dp(inits), ctypes.byref(out), cb, None)
+        else:
+            rc = fn(self._h, ctypes.byref(a), _dp(inits), _dp(im), ctypes.byref(out), cb, None)
+        _check(rc)
+        if mk == 1:
+            minv = minv.reshape(C, D, D)
+        return Fit(SAMPLER_COLUMNS + self.param_names, draws, eps, minv, tw, ts, ng, stt)
+
+    def transition(self, q0, p0, stepsize, inv_metric=None, metric="diag_e", max_depth=10, seed=0,
+                   chain_ids=None, counters=None):
+        """One NUTS transition per row of q0 with injected momenta p0."""
+        q0 = np.ascontiguousarray(np.atleast_2d(q0), dtype=np.float64)
+        p0 = np.ascontiguousarray(np.atleast_2d(p0), dtype=np.float64)
+        n = q0.shape[0]
+        mk = METRICS[metric]
+        im = None if inv_metric is None else np.ascontiguousarray(inv_metric, dtype=np.float64)
+        ids = np.ascontiguousarray(chain_ids if chain_ids is not None else np.arange(1, n + 1), dtype=np.uint32)
+        ctr = np.ascontiguousarray(counters if counters is not None else np.zeros(n), dtype=np.uint64)
+        qo = np.zeros((n, self.dim))
+        st = np.zeros((n, 7))
+        _check(self._lib.gnuts_transition(self._h, mk, _dp(im), n, _dp(q0), _dp(p0), float(stepsize), max_depth,
+                                          seed, ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
+                                          ctr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _dp(qo), _dp(st)))
+        return qo, st, ctr

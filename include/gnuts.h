@@ -1,0 +1,158 @@
+/*
+ * gnuts -- GB300-native NUTS sampler behind a plain C ABI.
+ *
+ * This is the drop-in boundary for CmdStan's sampling path.  Each entry
+ * point replaces one reference interface; the reference location is cited
+ * beside it (paths relative to the CmdStan source tree).  No C++ types,
+ * exceptions or device pointers cross this boundary: inputs and outputs are
+ * host arrays owned by the caller, errors are integer codes plus a message
+ * retrievable with gnuts_last_error().
+ *
+ * Threading: a model handle may be used by one thread at a time.
+ */
+#ifndef GNUTS_H
+#define GNUTS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes (0 = OK like stan::services::error_codes::OK;
+ *      src/cmdstan/return_codes.hpp:7 maps every non-zero to NOT_OK) ---- */
+#define GNUTS_OK 0
+#define GNUTS_ERR_ARGUMENT 1    /* invalid argument (bad value, bad combination) */
+#define GNUTS_ERR_DATA 2        /* missing / malformed data variable */
+#define GNUTS_ERR_INIT 3        /* initialisation failed (non-finite lp or gradient) */
+#define GNUTS_ERR_SAMPLER 4     /* sampler error (improper posterior, metric overflow) */
+#define GNUTS_ERR_CUDA 5        /* CUDA runtime error / no device */
+#define GNUTS_ERR_TIMEOUT 6     /* a bounded device wait ran out */
+
+/* gradient precision for data-heavy models */
+#define GNUTS_PRECISION_FP64 0   /* FP64 everywhere (CUDA cores) */
+#define GNUTS_PRECISION_MIXED 1  /* BF16 split-compensated tensor-core contractions, FP64 energy */
+
+/* ---- data: the C form of stan::io::var_context
+ *      (built by get_var_context, src/cmdstan/command_helper.hpp:116-133) ---- */
+#define GNUTS_VAR_INT 0
+#define GNUTS_VAR_REAL 1
+typedef struct {
+  const char* name;
+  int type;              /* GNUTS_VAR_INT (int32 data) or GNUTS_VAR_REAL (double data) */
+  int ndim;              /* 0 for scalars */
+  const int64_t* dims;   /* ndim extents, row-major data */
+  const void* data;
+} gnuts_var;
+
+typedef struct gnuts_model gnuts_model;
+
+/* Replaces new_model(var_context&, seed, &cout) (src/cmdstan/command.hpp:170-171)
+ * for the stanc-generated model.  model_id names one of the built-in models:
+ *   "bernoulli", "normal", "logistic", "hier", "funnel", "varint", "horseshoe". */
+int gnuts_model_create(const char* model_id, const gnuts_var* vars, int n_vars, unsigned int seed,
+                       gnuts_model** out);
+/* Same, with the data given as Stan JSON text (command_helper.hpp:116-133, JSON branch). */
+int gnuts_model_create_json(const char* model_id, const char* json_text, unsigned int seed,
+                            gnuts_model** out);
+void gnuts_model_destroy(gnuts_model* m);
+
+/* model_base::num_params_r and the number of write_array columns
+ * (command_helper.hpp:253-264). */
+int gnuts_model_dims(const gnuts_model* m, int* num_params_r, int* num_constrained);
+/* model_base::model_name (write_model.hpp) */
+int gnuts_model_name(const gnuts_model* m, char* buf, size_t len);
+/* model_base::constrained_param_names (unconstrained == 0) and
+ * unconstrained_param_names (unconstrained != 0), CSV spelling "beta.3" */
+int gnuts_model_param_name(const gnuts_model* m, int index, int unconstrained, char* buf, size_t len);
+
+/* stan::model::log_prob_grad<true, jacobian> at n points (command_helper.hpp:589-593),
+ * evaluated on the GPU.  q is n x num_params_r, grad is n x num_params_r. */
+int gnuts_log_prob_grad(const gnuts_model* m, int n, const double* q, int jacobian, double* lp,
+                        double* grad);
+/* model_base::transform_inits / unconstrain_array (command_helper.hpp:334-351) */
+int gnuts_unconstrain(const gnuts_model* m, const double* constrained, double* unconstrained);
+/* model_base::write_array for n unconstrained points -> n x num_constrained */
+int gnuts_write_array(const gnuts_model* m, int n, const double* q, double* out);
+
+/* ---- sampler arguments: the values command() reads for the sample branch
+ *      (src/cmdstan/command.hpp:554-655) ---- */
+typedef struct {
+  int num_chains;            /* num_chains (command_helper.hpp:613-642) */
+  unsigned int chain_id;     /* id: chain k has id chain_id + k */
+  unsigned int seed;         /* random seed */
+  double init_radius;        /* init = R (default 2); 0 = all zeros */
+  int num_warmup, num_samples, thin, save_warmup;
+  int refresh;               /* progress lines every `refresh` iterations (0 = none) */
+  double stepsize, stepsize_jitter;
+  int max_depth;
+  double delta, gamma, kappa, t0;
+  unsigned int init_buffer, term_buffer, window;
+  int precision;             /* GNUTS_PRECISION_* */
+} gnuts_sample_args;
+
+/* Fills the CmdStan defaults (arg_sample.hpp, arg_adapt.hpp, arg_hmc.hpp,
+ * arg_nuts.hpp, arg_init.hpp, arg_id.hpp, arg_seed.hpp). */
+void gnuts_sample_args_default(gnuts_sample_args* a);
+
+/* Outputs, all caller-allocated host arrays (NULL = not wanted).
+ * n_saved = (save_warmup ? ceil(num_warmup/thin) : 0) + ceil(num_samples/thin). */
+typedef struct {
+  double* draws;             /* [num_chains][n_saved][7 + num_constrained]: lp__, accept_stat__,
+                                stepsize__, treedepth__, n_leapfrog__, divergent__, energy__,
+                                then write_array values */
+  double* stepsize;          /* [num_chains] step size after adaptation */
+  double* inv_metric;        /* [num_chains][D] (diag/unit) or [num_chains][D][D] (dense) */
+  double* warmup_seconds;    /* [num_chains] */
+  double* sampling_seconds;  /* [num_chains] */
+  int64_t* n_grad;           /* [num_chains] gradient evaluations incl. init and step-size search */
+  int* chain_status;         /* [num_chains] GNUTS_OK or the chain's error code */
+} gnuts_output;
+
+/* Progress callback, called from the calling thread between device launches
+ * (mirrors the `Iteration: k / n [pct%]` logger lines). May be NULL. */
+typedef void (*gnuts_progress_fn)(void* ctx, int chain, int iteration, int total, int warmup);
+
+/* stan::services::sample::hmc_nuts_diag_e_adapt (command.hpp:673-688):
+ * inits NULL -> random inits; inv_metric NULL -> unit diagonal start
+ * (metric_file given -> command.hpp:673-680). */
+int gnuts_hmc_nuts_diag_e_adapt(gnuts_model* m, const gnuts_sample_args* a, const double* inits,
+                                const double* inv_metric, gnuts_output* out,
+                                gnuts_progress_fn progress, void* ctx);
+/* stan::services::sample::hmc_nuts_dense_e_adapt (command.hpp:657-672) */
+int gnuts_hmc_nuts_dense_e_adapt(gnuts_model* m, const gnuts_sample_args* a, const double* inits,
+                                 const double* inv_metric, gnuts_output* out,
+                                 gnuts_progress_fn progress, void* ctx);
+/* stan::services::sample::hmc_nuts_unit_e_adapt (command.hpp:689-697 branch) */
+int gnuts_hmc_nuts_unit_e_adapt(gnuts_model* m, const gnuts_sample_args* a, const double* inits,
+                                gnuts_output* out, gnuts_progress_fn progress, void* ctx);
+/* Non-adapting services hmc_nuts_{diag,dense,unit}_e (command.hpp:609-632) */
+int gnuts_hmc_nuts_diag_e(gnuts_model* m, const gnuts_sample_args* a, const double* inits,
+                          const double* inv_metric, gnuts_output* out, gnuts_progress_fn progress,
+                          void* ctx);
+int gnuts_hmc_nuts_dense_e(gnuts_model* m, const gnuts_sample_args* a, const double* inits,
+                           const double* inv_metric, gnuts_output* out, gnuts_progress_fn progress,
+                           void* ctx);
+int gnuts_hmc_nuts_unit_e(gnuts_model* m, const gnuts_sample_args* a, const double* inits,
+                          gnuts_output* out, gnuts_progress_fn progress, void* ctx);
+
+/* One NUTS transition per point with the momentum supplied (replay of
+ * base_nuts::transition with injected draws; no reference counterpart as an
+ * API, it exposes the transition that hmc_nuts_* run internally).
+ * metric: 0 diag, 1 dense, 2 unit.  inv_metric: D or D*D (shared by all points).
+ * counters[n]: stream-0 Philox draw counters, advanced on return.
+ * stats[n][7]: lp__, accept_stat__, stepsize__, treedepth__, n_leapfrog__, divergent__, energy__. */
+int gnuts_transition(gnuts_model* m, int metric, const double* inv_metric, int n, const double* q0,
+                     const double* p0, double stepsize, int max_depth, unsigned int seed,
+                     const unsigned int* chain_ids, uint64_t* counters, double* q_out, double* stats);
+
+/* Message of the last failing call on this thread. */
+int gnuts_last_error(char* buf, size_t len);
+/* Library version string, e.g. "gnuts 0.1 (sm_103a)". */
+const char* gnuts_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,230 @@
+"""GPU sampler vs the CPU oracle, through the C ABI.
+
+* log_prob_grad of every model: FP64, relative error <= 1e-10 (batched
+  round-mode path included for large N).
+* One NUTS transition with injected momentum (replay): identical tree depth,
+  leapfrog count, divergence flag and RNG consumption; selected point within
+  1e-10 relative.
+* Whole runs with adaptation on a Gaussian target (linear, non-chaotic
+  dynamics, so GPU and oracle stay together): draws, adapted step size and
+  inverse metric equal within 1e-8 relative for diag_e, dense_e and unit_e.
+* Whole runs on nonlinear models: moments within 4 combined MCSE of the
+  oracle, R-hat < 1.01, analytic posterior where one exists.
+"""
+import numpy as np
+import pytest
+
+import cmdstan_gb300 as gn
+from cmdstan_gb300 import workloads
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(mid, data):
+    return gn.Model(mid, data), oracle.OracleModel(mid, data)
+
+
+MODELS = [
+    ("bernoulli", workloads.bernoulli_reference()),
+    ("test_model", {}),
+    ("logistic", workloads.logistic(seed=3, N=300, D=7)),
+    ("logistic", workloads.logistic(seed=4, N=5000, D=20)),     # batched round-mode path
+    ("hier", workloads.eight_schools()),
+    ("hier", workloads.hier(seed=5, J=64)),
+    ("funnel", workloads.funnel(K=100)),
+    ("varint", workloads.varint(seed=6, J=12, K=10)),
+    ("horseshoe", workloads.horseshoe(seed=7, N=400, D=30, n_nonzero=4)),
+    ("horseshoe", workloads.horseshoe(seed=8, N=5000, D=40, n_nonzero=4)),  # batched
+]
+
+
+@pytest.mark.parametrize("mid,data", MODELS, ids=lambda v: v if isinstance(v, str) else "")
+@pytest.mark.parametrize("jac", [True, False])
+def test_log_prob_grad_matches_oracle(mid, data, jac):
+    gm, om = _pair(mid, data)
+    rng = np.random.default_rng(2)
+    q = rng.uniform(-1, 1, (5, gm.dim))
+    lp, g = gm.log_prob_grad(q, jacobian=jac)
+    for i in range(q.shape[0]):
+        olp, og = om.log_prob_grad(q[i], jac)
+        assert abs(lp[i] - olp) <= 1e-10 * max(1.0, abs(olp))
+        np.testing.assert_allclose(g[i], og, rtol=1e-10, atol=1e-10 * max(1.0, np.abs(og).max()))
+
+
+def test_write_array_matches_oracle():
+    for mid, data in MODELS[:1] + MODELS[4:5] + MODELS[7:9]:
+        gm, om = _pair(mid, data)
+        q = np.random.default_rng(3).uniform(-1, 1, (3, gm.dim))
+        out = gm.write_array(q)
+        for i in range(3):
+            np.testing.assert_allclose(out[i], om.write_array(q[i]), rtol=1e-12)
+
+
+REPLAY = [
+    ("test_model", {}, 0.9, "diag_e"),
+    ("test_model", {}, 0.05, "diag_e"),      # long trajectories: max depth
+    ("test_model", {}, 40.0, "diag_e"),      # divergences
+    ("test_model", {}, 0.7, "dense_e"),
+    ("test_model", {}, 0.7, "unit_e"),
+    ("bernoulli", workloads.bernoulli_reference(), 1.0, "diag_e"),
+    ("hier", workloads.eight_schools(), 0.3, "diag_e"),
+    ("hier", workloads.eight_schools(), 0.3, "dense_e"),
+    ("funnel", workloads.funnel(K=20), 0.2, "diag_e"),
+    ("logistic", workloads.logistic(seed=3, N=300, D=7), 0.1, "diag_e"),
+    ("varint", workloads.varint(seed=6, J=5, K=3), 0.05, "diag_e"),
+    ("horseshoe", workloads.horseshoe(seed=7, N=200, D=6, n_nonzero=2), 0.05, "diag_e"),
+]
+
+
+@pytest.mark.parametrize("mid,data,eps,metric", REPLAY, ids=lambda v: str(v) if not isinstance(v, dict) else "")
+def test_transition_replay_matches_oracle(mid, data, eps, metric):
+    gm, om = _pair(mid, data)
+    D = gm.dim
+    rng = np.random.default_rng(5)
+    n = 24
+    q0 = rng.uniform(-1, 1, (n, D))
+    p0 = rng.standard_normal((n, D))
+    mk = gn.METRICS[metric]
+    if mk == 0:
+        im = rng.uniform(0.5, 2.0, D)
+    elif mk == 1:
+        A = rng.standard_normal((D, D)) * 0.2
+        im = A @ A.T + np.eye(D)
+    else:
+        im = None
+    ids = np.arange(7, 7 + n, dtype=np.uint32)
+    ctr = rng.integers(0, 1000, n).astype(np.uint64)
+    qo, st, ctr_out = gm.transition(q0, p0, eps, inv_metric=None if im is None else im.ravel(), metric=metric,
+                                    max_depth=6, seed=99, chain_ids=ids, counters=ctr.copy())
+    for i in range(n):
+        oq, ost, octr = om.transition(q0[i], p0[i], eps, inv_metric=None if im is None else im.ravel(), metric=mk,
+                                      max_depth=6, seed=99, chain=int(ids[i]), counter=int(ctr[i]))
+        assert st[i, 3] == ost[3], "treedepth"
+        assert st[i, 4] == ost[4], "n_leapfrog"
+        assert st[i, 5] == ost[5], "divergent"
+        assert int(ctr_out[i]) == octr, "rng draws consumed"
+        np.testing.assert_allclose(qo[i], oq, rtol=1e-10, atol=1e-10)
+        np.testing.assert_allclose(st[i, [0, 1, 6]], ost[[0, 1, 6]], rtol=1e-9, atol=1e-9)
+
+
+GAUSS = {"scales": np.array([1.0, 3.0, 0.5, 2.0, 1.5])}
+
+
+@pytest.mark.parametrize("metric", ["diag_e", "dense_e", "unit_e"])
+def test_full_run_gaussian_equals_oracle(metric):
+    """Adaptation, windows, step-size search, RNG schedule and draw recording
+    end to end: on a Gaussian target the GPU run equals the oracle run."""
+    gm, om = _pair("normal", GAUSS)
+    kw = dict(num_warmup=300, num_samples=200, seed=4321)
+    fit = gm.sample(metric=metric, num_chains=3, chain_id=1, **kw)
+    od, oeps, ominv, ong = om.run_chains(3, threads=3, first_chain_id=1, metric=gn.METRICS[metric], **kw)
+    np.testing.assert_allclose(fit.stepsize, oeps, rtol=1e-8)
+    np.testing.assert_allclose(fit.inv_metric.reshape(3, -1), ominv, rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(fit.draws[:, :, :7], od[:, :, :7], rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(fit.draws[:, :, 7:], od[:, :, 7:], rtol=1e-8, atol=1e-10)
+    # n_grad on the device also counts the initial gradient
+    assert np.all(fit.n_grad == ong)
+
+
+def test_full_run_save_warmup_thin_and_no_adapt():
+    gm, om = _pair("normal", GAUSS)
+    kw = dict(num_warmup=120, num_samples=90, seed=77, save_warmup=1, thin=4)
+    fit = gm.sample(num_chains=2, **kw)
+    od, oeps, _, _ = om.run_chains(2, threads=2, **kw)
+    assert fit.draws.shape[1] == 30 + 23
+    np.testing.assert_allclose(fit.draws, od, rtol=1e-8, atol=1e-10)
+    fit = gm.sample(adapt=False, num_chains=2, stepsize=0.37, num_warmup=20, num_samples=50, seed=5)
+    od, oeps, _, _ = om.run_chains(2, threads=2, adapt_engaged=0, stepsize=0.37, num_warmup=20, num_samples=50,
+                                   seed=5)
+    assert np.all(fit.draws[:, :, 2] == 0.37) and np.all(fit.stepsize == 0.37)
+    np.testing.assert_allclose(fit.draws, od, rtol=1e-8, atol=1e-10)
+
+
+def test_bernoulli_posterior_and_oracle():
+    gm, om = _pair("bernoulli", workloads.bernoulli_reference())
+    fit = gm.sample(num_chains=4, seed=1234)
+    th = fit.column("theta")
+    s = oracle.summary(th)
+    # Beta(3, 9) posterior; the reference's own bound (stansummary_test.cpp:249-253) is (0.25, 0.27)
+    assert abs(s["mean"] - 0.25) < 3 * s["mcse"] + 1e-3
+    assert s["rhat"] < 1.01
+    od, oeps, ominv, _ = om.run_chains(4, threads=4, seed=1234)
+    os_ = oracle.summary(1 / (1 + np.exp(-od[:, :, 7])))
+    assert abs(s["mean"] - os_["mean"]) < 4 * np.hypot(s["mcse"], os_["mcse"])
+    assert abs(np.median(fit.stepsize) - np.median(oeps)) < 0.5
+    assert np.all(fit.draws[:, :, 3] >= 1) and np.all(fit.draws[:, :, 4] >= 1)
+
+
+@pytest.mark.parametrize("mid,data,kw", [
+    ("hier", workloads.eight_schools(), dict(delta=0.95)),
+    ("funnel", workloads.funnel(K=10), dict(delta=0.9)),
+    ("logistic", workloads.logistic(seed=3, N=500, D=5), {}),
+    ("logistic", workloads.logistic(seed=4, N=5000, D=10), {}),
+    ("varint", workloads.varint(seed=9, J=8, K=3), {}),
+    ("horseshoe", workloads.horseshoe(seed=10, N=300, D=8, n_nonzero=2), dict(delta=0.95)),
+], ids=lambda v: v if isinstance(v, str) else "")
+def test_moments_match_oracle(mid, data, kw):
+    gm, om = _pair(mid, data)
+    C = 8
+    fit = gm.sample(num_chains=C, seed=2024, **kw)
+    od, _, _, _ = om.run_chains(C, threads=8, seed=2024, **kw)
+    cons = np.array([[om.write_array(od[c, i, 7:]) for i in range(od.shape[1])] for c in range(C)])
+    checked = 0
+    for j in range(min(gm.num_constrained, 12)):
+        x, y = fit.draws[:, :, 7 + j], cons[:, :, j]
+        sx, sy = oracle.summary(x), oracle.summary(y)
+        if mid != "funnel" and mid != "hier":
+            assert sx["rhat"] < 1.01, (j, sx["rhat"])
+        tol = 4.5 * np.hypot(sx["mcse"], sy["mcse"])
+        assert abs(sx["mean"] - sy["mean"]) < tol, (gm.param_names[j], sx["mean"], sy["mean"], tol)
+        checked += 1
+    assert checked > 0
+
+
+def test_seed_determinism():
+    gm = gn.Model("hier", workloads.eight_schools())
+    a = gm.sample(num_chains=2, seed=11, num_warmup=200, num_samples=100)
+    b = gm.sample(num_chains=2, seed=11, num_warmup=200, num_samples=100)
+    c = gm.sample(num_chains=2, seed=12, num_warmup=200, num_samples=100)
+    assert np.array_equal(a.draws, b.draws)
+    assert not np.array_equal(a.draws, c.draws)
+    lg = gn.Model("logistic", workloads.logistic(seed=4, N=5000, D=10))
+    a = lg.sample(num_chains=4, seed=3, num_warmup=100, num_samples=50)
+    b = lg.sample(num_chains=4, seed=3, num_warmup=100, num_samples=50)
+    assert np.array_equal(a.draws, b.draws)
+
+
+def test_chain_ids_offset_draws():
+    gm = gn.Model("proper")
+    a = gm.sample(num_chains=3, chain_id=10, seed=5, num_warmup=50, num_samples=20)
+    b = gm.sample(num_chains=1, chain_id=11, seed=5, num_warmup=50, num_samples=20)
+    np.testing.assert_array_equal(a.draws[1], b.draws[0])
+
+
+def test_init_failure_reports_error():
+    gm = gn.Model("funnel", workloads.funnel(K=3))
+    with pytest.raises(gn.GnutsError) as e:
+        gm.sample(num_chains=1, inits=np.array([-1e4, 1.0, 1.0, 1.0]), num_warmup=10, num_samples=10)
+    assert e.value.code == gn.gnuts.ERR_INIT
+    assert "Initialization failed" in e.value.msg
+
+
+def test_user_inits_and_init_zero():
+    gm = gn.Model("test_model")
+    fit = gm.sample(num_chains=2, inits=np.array([1.0, -1.0]), adapt=False, num_warmup=0, num_samples=5, seed=1)
+    assert fit.draws.shape == (2, 5, 9)
+    fit = gm.sample(num_chains=1, init_radius=0.0, num_warmup=30, num_samples=5, seed=1)
+    assert np.all(np.isfinite(fit.draws))
+
+
+def test_fp32_batched_gradient_close_to_fp64():
+    data = workloads.logistic(seed=4, N=8192, D=32)
+    gm, om = _pair("logistic", data)
+    q = np.random.default_rng(1).normal(0, 0.2, (3, gm.dim))
+    fit = gm.sample(num_chains=4, seed=1, num_warmup=150, num_samples=100, precision=gn.PRECISION_MIXED)
+    assert np.all(np.isfinite(fit.draws))
+    lp, g = gm.log_prob_grad(q)
+    for i in range(3):
+        olp, og = om.log_prob_grad(q[i])
+        assert abs(lp[i] - olp) < 1e-9 * abs(olp)

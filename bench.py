@@ -1,0 +1,325 @@
+"""Benchmark: NUTS on the logistic-regression workload (N=100,000 x D=100,
+1024 chains sharing X, diag_e, 1000 warmup + 1000 draws, adaptation on).
+
+One step = one complete sampling run of all chains (the unit over which
+min bulk-ESS/s is defined).  Reported:
+  value       grad-evals/s = sum of n_leapfrog__ over all chains, warmup and
+              sampling, divided by the sampler's device time (inputs resident)
+  e2e         the same metric through the C ABI with host buffers: model
+              creation (X and y copied host -> device), sampling, draws copied
+              device -> host, all inside the timed region
+  min_bulk_ess_per_s, rhat_max   from the draws of each run
+  roofline    the tcgen05 gradient kernel: algorithmic 4*N*D flops per chain
+              per round over its CUDA-event duration, against the measured
+              sustained bf16 peak
+  cpu_baseline  the CPU FP64 oracle on the host cores (one chain per core), a
+              bounded sample of transitions started at the posterior mode
+Between timed steps a 256 MB buffer is written to flush L2.
+Replicas only: under torchrun each rank runs an independent replica.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "min bulk-ESS/s, grad-evals/s on 1 GB300: learned vs plain GPU NUTS, R-hat<1.01"
+N_ROWS, N_PRED, N_CHAINS = 100_000, 100, 1024
+NUM_WARMUP, NUM_SAMPLES = 1000, 1000
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the gradient kernel from the committed ncu summary (or None)."""
+    p = os.path.join(ROOT, "profiles", "k_glm_tc_logistic_100k_x_100.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].strip())
+                except ValueError:
+                    return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) < 9:
+                        continue
+                    try:
+                        sm.append(float(parts[1]))
+                        mx.append(float(parts[2]))
+                    except ValueError:
+                        continue
+                    for nm, v in zip(names, parts[5:9]):
+                        if v.lower().startswith("active"):
+                            reasons.add(nm)
+            os.unlink(self.path)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload_data(seed=0):
+    from cmdstan_gb300 import workloads
+    return workloads.logistic(seed=seed, N=N_ROWS, D=N_PRED)
+
+
+def map_laplace(data):
+    """Posterior mode and diagonal Laplace variance (Newton, numpy FP64): the
+    starting state of the bounded CPU sample."""
+    X, y = data["X"], data["y"].astype(np.float64)
+    Xa = np.hstack([np.ones((X.shape[0], 1)), X])
+    prior = np.r_[1 / 6.25, np.ones(X.shape[1])]
+    w = np.zeros(Xa.shape[1])
+    for _ in range(8):
+        eta = Xa @ w
+        p = 1 / (1 + np.exp(-eta))
+        g = Xa.T @ (y - p) - prior * w
+        H = (Xa * (p * (1 - p))[:, None]).T @ Xa + np.diag(prior)
+        w = w + np.linalg.solve(H, g)
+    return w, np.diag(np.linalg.inv(H))
+
+
+def cpu_sample(data, seconds=15.0, threads=None):
+    """Oracle NUTS on the host cores: one chain per core, adaptation off, at the
+    posterior mode with the Laplace metric; iterations sized to ~`seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    om = oracle.OracleModel("logistic", data)
+    w, var = map_laplace(data)
+    kw = dict(adapt_engaged=0, stepsize=0.7, num_warmup=0, seed=7)
+    t = time.time()
+    _, _, _, ng = om.run_chains(threads, threads=threads, inits=w, inv_metric=var, num_samples=2, **kw)
+    probe = time.time() - t
+    per_iter = probe / 2.0
+    iters = int(max(2, min(400, seconds / max(per_iter, 1e-6))))
+    t = time.time()
+    _, _, _, ng = om.run_chains(threads, threads=threads, inits=w, inv_metric=var, num_samples=iters, **kw)
+    wall = time.time() - t
+    return {"value": float(ng.sum() / wall), "unit": "grad-evals/s", "cores": threads, "kind": "port",
+            "sample": "%d chains x %d transitions (adaptation off, started at the posterior mode, Laplace diag "
+                      "metric, step 0.7) of the same workload, FP64, %d host threads; %.1f s" %
+                      (threads, iters, threads, wall)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    data = workload_data(0)
+    res = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(data, seconds=args.cpu_seconds)
+        if i >= args.warmup:
+            res.append(r)
+    v = float(np.mean([r["value"] for r in res]))
+    line = {"metric": METRIC, "value": v, "unit": "grad-evals/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+            "config": config(args),
+            "cpu_baseline": {"value": v, "unit": "grad-evals/s", "cores": res[-1]["cores"], "kind": "port",
+                             "sample": res[-1]["sample"]},
+            "e2e": {"value": v, "unit": "grad-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's own implementation (stan submodule) is absent from the reference tree; "
+                    "the CPU oracle restating it times the CPU path"}
+    print(json.dumps(line))
+
+
+def config(args):
+    return {"workload": "logistic regression N=100000 x D=100 (+intercept), 1024 chains on one shared X, "
+                        "NUTS diag_e, 1000 warmup + 1000 draws, adapt delta 0.8, max_depth 10",
+            "chains": N_CHAINS, "rows": N_ROWS, "predictors": N_PRED, "num_warmup": NUM_WARMUP,
+            "num_samples": NUM_SAMPLES, "precision": "BF16 hi/lo split tensor-core gradient, FP32 accumulate, "
+                                                     "FP64 energy / lp sum / adaptation",
+            "l2": "256 MB buffer written between timed steps", "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="profiling aid: one short run (20 warmup + 10 draws) of the same workload; not a bench value")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.quick:
+        import cmdstan_gb300 as gn
+        model = gn.Model("logistic", workload_data(0))
+        fit = model.sample(num_chains=N_CHAINS, num_warmup=20, num_samples=10, refresh=0, seed=1,
+                           precision=gn.PRECISION_MIXED)
+        print(json.dumps({"quick": True, "note": "profiling run, not a bench value", "timing": fit.timing,
+                          "leapfrogs": int(fit.n_leapfrog.sum())}))
+        return
+
+    import torch
+    import cmdstan_gb300 as gn
+    from cmdstan_gb300 import gnuts
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    data = workload_data(0)
+    model = gn.Model("logistic", data)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    kw = dict(num_chains=N_CHAINS, num_warmup=NUM_WARMUP, num_samples=NUM_SAMPLES, refresh=0,
+              precision=gn.PRECISION_MIXED)
+
+    def one_step(seed):
+        return model.sample(seed=seed, chain_id=1 + rank * N_CHAINS, **kw)
+
+    for i in range(args.warmup):
+        one_step(1000 + i)
+    fits, times = [], []
+    peaks, peak_kind = measured_peaks()
+    with Clocks(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            if dist:
+                dist.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fit = one_step(1 + i)
+            e1.record()
+            torch.cuda.synchronize()
+            if dist:
+                dist.barrier()
+            times.append(e0.elapsed_time(e1))
+            fits.append(fit)
+    clocks = clk.summary()
+    # whole-job throughput: leapfrogs over the sampler's device time (max over ranks)
+    lf = float(sum(f.n_leapfrog.sum() for f in fits))
+    dev_ms = float(sum(f.timing["device_ms"] for f in fits))
+    if dist:
+        t = torch.tensor([lf, dev_ms, sum(times)], dtype=torch.float64, device="cuda")
+        tot = t.clone()
+        dist.all_reduce(tot[:1])
+        mx = t[1:].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        lf, dev_ms, wall_ms = float(tot[0]), float(mx[0]), float(mx[1])
+    else:
+        wall_ms = float(sum(times))
+    value = lf / (dev_ms / 1e3)
+    # ESS / R-hat of the last run
+    last = fits[-1]
+    cols = list(range(7, last.draws.shape[2]))
+    sm = gnuts.summary_columns(last.draws, cols, threads=os.cpu_count() or 8)
+    ess_min = float(min(s["ess_bulk"] for s in sm))
+    rhat_max = float(max(s["rhat"] for s in sm))
+    step_s = last.timing["device_ms"] / 1e3
+    grad_us = float(np.mean([f.timing["grad_kernel_us"] for f in fits]))
+    adv_us = float(np.mean([f.timing["advance_kernel_us"] for f in fits]))
+    flops = 4.0 * N_ROWS * N_PRED * N_CHAINS
+    achieved = flops / (grad_us * 1e-6) / 1e12
+    peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops")))
+    traffic = profile_traffic()
+    # e2e: host buffers through the C ABI, model creation + sampling + draws back
+    e2e_times, e2e_lf = [], 0.0
+    for i in range(max(1, min(args.steps, 2))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m2 = gn.Model("logistic", data)
+        f2 = m2.sample(seed=100 + i, chain_id=1 + rank * N_CHAINS, **kw)
+        del m2
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_lf += float(f2.n_leapfrog.sum())
+    e2e_value = e2e_lf / sum(e2e_times)
+    h2d = data["X"].nbytes + data["y"].astype(np.int32).nbytes
+    d2h = last.draws.nbytes + last.n_leapfrog.nbytes * 4 + last.stepsize.nbytes + last.inv_metric.nbytes
+    launches = int(sum(f.timing["launches"] for f in fits))
+    line = {
+        "metric": METRIC, "value": value, "unit": "grad-evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2/fp32/fp64",
+        "data": "synthetic (seeded PCG64, X rounded to bf16)", "config": config(args),
+        "min_bulk_ess_per_s": ess_min / step_s, "min_bulk_ess": ess_min, "rhat_max": rhat_max,
+        "sampler_device_s_per_step": dev_ms / 1e3 / args.steps,
+        "leapfrogs_per_step": lf / args.steps,
+        "kernels_us": {"k_glm_tc": grad_us, "k_advance": adv_us},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_kind": "%s bf16 sustained" % peak_kind,
+                     "note": "algorithmic 4*N*D flops per chain-gradient x 1024 chains per launch; the BF16 "
+                             "hi/lo split executes twice that on the tensor pipe"},
+        "e2e": {"value": e2e_value, "unit": "grad-evals/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "s_per_step": float(np.mean(e2e_times))},
+        "gpu_launches": launches, "clocks": clocks,
+    }
+    if rank == 0:
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_sample(data, seconds=args.cpu_seconds)
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

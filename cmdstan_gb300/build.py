@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-I" + CSRC]
 
 CU_SOURCES = ["sampler.cu", "grad_tc.cu"]
-CPP_SOURCES = ["abi.cpp"]
+CPP_SOURCES = ["abi.cpp", "summary.cpp"]
 
 
 def _nvcc():

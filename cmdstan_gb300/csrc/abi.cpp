@@ -526,7 +526,17 @@ int gnuts_model_param_name(const gnuts_model* m, int index, int unconstrained, c
 int gnuts_log_prob_grad(const gnuts_model* m, int n, const double* q, int jacobian, double* lp, double* grad) {
   if (!m || (n > 0 && (!q || !lp || !grad))) return fail(GNUTS_ERR_ARGUMENT, "null argument");
   std::string err;
-  int rc = run_log_prob_grad(*const_cast<Model*>(M(m)), n, q, jacobian, lp, grad, err);
+  int rc = run_log_prob_grad(*const_cast<Model*>(M(m)), n, q, jacobian, GNUTS_PRECISION_FP64, lp, grad, err);
+  return rc ? fail(rc, err) : GNUTS_OK;
+}
+
+int gnuts_log_prob_grad_precision(const gnuts_model* m, int n, const double* q, int jacobian, int precision,
+                                  double* lp, double* grad) {
+  if (!m || (n > 0 && (!q || !lp || !grad))) return fail(GNUTS_ERR_ARGUMENT, "null argument");
+  if (precision != GNUTS_PRECISION_FP64 && precision != GNUTS_PRECISION_MIXED)
+    return fail(GNUTS_ERR_ARGUMENT, "unknown precision");
+  std::string err;
+  int rc = run_log_prob_grad(*const_cast<Model*>(M(m)), n, q, jacobian, precision, lp, grad, err);
   return rc ? fail(rc, err) : GNUTS_OK;
 }
 

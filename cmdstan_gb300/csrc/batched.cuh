@@ -18,6 +18,7 @@
 // partial sums to [S][C] / [S][C][K+1] buffers which reduce_gradient sums in
 // a fixed order, so results are bitwise reproducible run to run.
 #pragma once
+#include <cuda_bf16.h>
 #include "device_models.cuh"
 
 namespace gnuts {
@@ -33,7 +34,9 @@ struct GradOut {
   double* part_g;   // [S][C][K+1]
   const int* done_count;
   int C_total;
-  void* tc;         // tensor-core path state (grad_tc.cu)
+  void* tc;           // tensor-core plan (grad_tc.cu), null for the SIMT path
+  uint16_t* coef_bf;  // tensor-core operand: [2][Cpad][128] BF16 hi / lo planes
+  int Cpad;
 };
 
 inline bool batched_supported(const DevModel& M) {
@@ -48,6 +51,19 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
   double* o64 = G.coef64 + (size_t)c * (K + 1);
   float* o32 = G.coef32 ? G.coef32 + (size_t)c * (K + 1) : nullptr;
   if (M.kind == MK_LOGISTIC) {
+    if (G.coef_bf) {
+      // tensor-core operand: column k < K -> beta_k, column K -> intercept (it
+      // meets the ones column of X), split v = hi + lo in BF16
+      __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(G.coef_bf) + (size_t)c * 128;
+      __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(G.coef_bf) + ((size_t)G.Cpad + c) * 128;
+      for (int i = lane; i < 128; i += 32) {
+        double v = i < K ? q[1 + i] : (i == K ? q[0] : 0.0);
+        __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
+      }
+      return;
+    }
     for (int i = lane; i <= K; i += 32) {
       double v = q[i];
       o64[i] = v;
@@ -197,10 +213,22 @@ __global__ void __launch_bounds__(GLM_THREADS) k_glm_simt(GradOut G, DevModel M)
       const int n = r0 + er, c = c0 + ec;
       T r = 0;
       if (n < row_end && c < G.C) {
-        double e = (double)eta + (double)coef[(size_t)c * (K + 1)];
-        int y = M.yi[n];
-        lp_acc += y * e - log1p_exp(e);
-        r = (T)(y - inv_logit(e));
+        const int y = M.yi[n];
+        if constexpr (sizeof(T) == 8) {
+          double e = eta + coef[(size_t)c * (K + 1)];
+          lp_acc += y * e - log1p_exp(e);
+          r = y - inv_logit(e);
+        } else {
+          // FP32 elementwise step (FP64 is scarce on this part); the sum stays FP64
+          float e = eta + coef[(size_t)c * (K + 1)];
+          float ax = fabsf(e);
+          float l1p = log1pf(__expf(-ax));            // log1p(exp(-|e|))
+          float term = (y ? fminf(e, 0.f) : -fmaxf(e, 0.f)) - l1p;  // y e - log1p_exp(e)
+          lp_acc += (double)term;
+          float s = 1.f / (1.f + __expf(-ax));         // inv_logit(|e|)
+          float il = e >= 0.f ? s : 1.f - s;
+          r = (float)y - il;
+        }
       }
       rs[ec][er] = r;
     }

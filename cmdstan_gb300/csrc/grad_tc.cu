@@ -1,3 +1,497 @@
-// Tensor-core (tcgen05) contraction for the batched logistic gradient.
-// Placeholder translation unit; the kernel lands here.
-#include "internal.h"
+// tcgen05 tensor-core kernel for the batched logistic-regression gradient.
+//
+// Per round every live chain c needs, for its coefficients B_c (intercept
+// folded in through a ones column of X),
+//     H[c, n] = B_c . X_n                       GEMM1, M = chains, N = rows, K = predictors
+//     lp_c    = -sum_n softplus(s_n H[c, n]),   s_n = 1 - 2 y_n
+//     R[c, n] = -s_n inv_logit(s_n H[c, n])     (= y_n - inv_logit(H[c, n]))
+//     G[c, k] = sum_n R[c, n] X[n, k]           GEMM2, M = chains, N = predictors, K = rows
+// which is the reverse sweep Stan Math performs for one chain's
+// bernoulli_logit likelihood (log_prob_grad contract, src/cmdstan/
+// command_helper.hpp:589-593), done for 128 chains at once.
+//
+// Precision: X is BF16-exact (the workload's design matrix is defined on
+// BF16 values).  Coefficients and residuals are split hi + lo in BF16, so
+// each contraction is two BF16 MMAs accumulated in FP32 TMEM (about 16
+// significant bits per operand).  softplus / inv_logit run in FP32; each
+// thread Kahan-sums its 64-row slice of lp in FP32 and adds it to an FP64
+// accumulator; the reduction over row splits is FP64 in the advance kernel.
+//
+// CTA = one 128-chain tile x one row split, 320 threads:
+//   warp 0      TMA producer: coefficient hi/lo tiles once, X row tiles
+//               (2-stage ring, 128 rows x 128 predictors, SWIZZLE_128B)
+//   warp 1      MMA issuer (one thread) + TMEM owner
+//   warps 2..9  epilogue: thread = (chain, half of the 128-row tile);
+//               reads its H slice from TMEM, writes R hi/lo into shared
+//               memory in the SW128 K-major layout GEMM2 reads
+// TMEM: H double buffer (2 x 128 columns) + G (128 columns).
+// Every mbarrier wait is bounded; on expiry the kernel records an error,
+// drains what it issued and frees TMEM.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstring>
+#include <string>
+#include "grad_tc.h"
+
+namespace gnuts {
+namespace {
+
+constexpr int TILE_BYTES = 128 * 128 * 2;   // [2 k-halves][128 rows][64] BF16
+constexpr int HALF_BYTES = TILE_BYTES / 2;  // one k-half: 128 rows x 128 B
+constexpr int NS = 2;
+constexpr int NUM_THREADS = 320;
+constexpr int OFF_CHI = 0;
+constexpr int OFF_CLO = OFF_CHI + TILE_BYTES;
+constexpr int OFF_X = OFF_CLO + TILE_BYTES;
+constexpr int OFF_RHI = OFF_X + NS * TILE_BYTES;
+constexpr int OFF_RLO = OFF_RHI + TILE_BYTES;
+constexpr int OFF_BAR = OFF_RLO + TILE_BYTES;  // 16 barriers
+constexpr int OFF_MISC = OFF_BAR + 16 * 8;     // tmem base, abort flag
+constexpr int OFF_LP = OFF_MISC + 16;          // [2][128] doubles
+constexpr int SMEM_USED = OFF_LP + 2 * 128 * 8;
+constexpr int SMEM_BYTES = SMEM_USED + 1024;   // alignment slack
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t SPIN_LIMIT = 1u << 22;
+
+// barrier indices
+enum { B_XFULL = 0, B_XEMPTY = NS, B_CFULL = 2 * NS, B_HFULL, B_HFULL1, B_HEMPTY, B_HEMPTY1, B_RFULL, B_REMPTY,
+       B_GDONE, B_DRAIN };
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// bounded wait for the phase with the given parity; false on timeout / abort
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
+  for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if ((i & 255u) == 255u && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor: SWIZZLE_128B, descriptor version 1
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+// instruction descriptor, kind::f16: D FP32, A/B BF16, M = 128, N = 128
+__host__ __device__ constexpr uint32_t idesc(bool a_mn, bool b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+         ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(id), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+struct TcArgs {
+  int N, K, C, Cpad, rows_per_split, S, C_total;
+  const uint32_t* ybits;
+  double* part_lp;
+  double* part_g;
+  const int* done_count;
+  int* error;
+};
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_glm_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap, TcArgs A) {
+  if (A.done_count && *A.done_count >= A.C_total) return;
+  extern __shared__ uint8_t smem_raw[];
+  // SWIZZLE_128B tiles need 1024-byte alignment in the shared address space
+  uint8_t* smem = smem_raw + ((1024u - (su32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = su32(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c0 = blockIdx.x * 128;
+  const int split = blockIdx.y;
+  const int row_begin = split * A.rows_per_split;
+  const int row_end = min(A.N, row_begin + A.rows_per_split);
+  const int T = row_end > row_begin ? (row_end - row_begin + 127) / 128 : 0;
+  auto bar = [&](int i) { return sbase + OFF_BAR + 8u * (uint32_t)i; };
+  volatile int* abort = (volatile int*)(smem + OFF_MISC + 4);
+  uint32_t* tmem_slot = (uint32_t*)(smem + OFF_MISC);
+  double* lpx = (double*)(smem + OFF_LP);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(bar(B_XFULL + s), 1);
+      mbar_init(bar(B_XEMPTY + s), 1);
+    }
+    mbar_init(bar(B_CFULL), 1);
+    mbar_init(bar(B_HFULL), 1);
+    mbar_init(bar(B_HFULL1), 1);
+    mbar_init(bar(B_HEMPTY), 8);
+    mbar_init(bar(B_HEMPTY1), 8);
+    mbar_init(bar(B_RFULL), 8);
+    mbar_init(bar(B_REMPTY), 1);
+    mbar_init(bar(B_GDONE), 1);
+    mbar_init(bar(B_DRAIN), 1);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer
+    if (lane == 0) {
+      int issued = 0;
+      mbar_expect_tx(bar(B_CFULL), 2 * TILE_BYTES);
+      tma_load_2d(sbase + OFF_CHI, &cmap, 0, c0, bar(B_CFULL));
+      tma_load_2d(sbase + OFF_CHI + HALF_BYTES, &cmap, 64, c0, bar(B_CFULL));
+      tma_load_2d(sbase + OFF_CLO, &cmap, 0, A.Cpad + c0, bar(B_CFULL));
+      tma_load_2d(sbase + OFF_CLO + HALF_BYTES, &cmap, 64, A.Cpad + c0, bar(B_CFULL));
+      for (int t = 0; t < T; ++t) {
+        const int s = t % NS;
+        if (t >= NS && !mbar_wait(bar(B_XEMPTY + s), ((t / NS) - 1) & 1, abort)) break;
+        const uint32_t dst = sbase + OFF_X + s * TILE_BYTES;
+        mbar_expect_tx(bar(B_XFULL + s), TILE_BYTES);
+        tma_load_2d(dst, &xmap, 0, row_begin + t * 128, bar(B_XFULL + s));
+        tma_load_2d(dst + HALF_BYTES, &xmap, 64, row_begin + t * 128, bar(B_XFULL + s));
+        ++issued;
+      }
+      if (*abort) {
+        // drain: wait (bounded) for every load issued into the ring
+        for (int t = (issued > NS ? issued - NS : 0); t < issued; ++t) {
+          volatile int never = 0;
+          mbar_wait(bar(B_XFULL + t % NS), (t / NS) & 1, &never);
+        }
+        volatile int never = 0;
+        mbar_wait(bar(B_CFULL), 0, &never);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      const uint32_t ID1 = idesc(false, false);  // A coef K-major, B = X K-major
+      const uint32_t ID2 = idesc(false, true);   // A = R K-major, B = X MN-major
+      const uint32_t tG = tmem + 256;
+      bool ok = mbar_wait(bar(B_CFULL), 0, abort);
+      auto gemm2 = [&](int u) -> bool {
+        if (!mbar_wait(bar(B_RFULL), u & 1, abort)) return false;
+        fence_after();
+        const uint32_t xs = sbase + OFF_X + (u % NS) * TILE_BYTES;
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+          const uint32_t rs = sbase + (part ? OFF_RLO : OFF_RHI);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            uint64_t a = sdesc(rs + (i >> 2) * HALF_BYTES + (i & 3) * 32, 0, 1024);
+            uint64_t b = sdesc(xs + i * 2048, HALF_BYTES, 1024);
+            mma(tG, a, b, ID2, (u > 0 || part > 0 || i > 0) ? 1u : 0u);
+          }
+        }
+        mma_commit(bar(B_XEMPTY + u % NS));
+        mma_commit(bar(B_REMPTY));
+        return true;
+      };
+      int t = 0;
+      for (; ok && t < T; ++t) {
+        const int s = t % NS, b = t & 1;
+        if (!mbar_wait(bar(B_XFULL + s), (t / NS) & 1, abort)) { ok = false; break; }
+        if (t >= 2 && !mbar_wait(bar(B_HEMPTY + b), ((t >> 1) - 1) & 1, abort)) { ok = false; break; }
+        fence_after();
+        const uint32_t xs = sbase + OFF_X + s * TILE_BYTES;
+        const uint32_t tH = tmem + b * 128;
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+          const uint32_t cs = sbase + (part ? OFF_CLO : OFF_CHI);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const uint32_t koff = (i >> 2) * HALF_BYTES + (i & 3) * 32;
+            mma(tH, sdesc(cs + koff, 0, 1024), sdesc(xs + koff, 0, 1024), ID1, (part > 0 || i > 0) ? 1u : 0u);
+          }
+        }
+        mma_commit(bar(B_HFULL + b));
+        if (t >= 1 && !gemm2(t - 1)) { ok = false; break; }
+      }
+      if (ok && T > 0) ok = gemm2(T - 1);
+      mma_commit(bar(B_GDONE));
+      // drain every MMA this thread issued before TMEM is released
+      mma_commit(bar(B_DRAIN));
+      volatile int never = 0;
+      mbar_wait(bar(B_DRAIN), 0, &never);
+    }
+  } else {
+    // ---------------- epilogue: 8 warps, thread = (chain, row half)
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    const int cl = q * 32 + lane;  // chain within the tile
+    const int c = c0 + cl;
+    double lp_acc = 0.0;
+    uint8_t* rhi = smem + OFF_RHI + half * HALF_BYTES + cl * 128;
+    uint8_t* rlo = smem + OFF_RLO + half * HALF_BYTES + cl * 128;
+    bool ok = true;
+    for (int t = 0; t < T && ok; ++t) {
+      const int b = t & 1;
+      if (!mbar_wait(bar(B_HFULL + b), (t >> 1) & 1, abort)) { ok = false; break; }
+      fence_after();
+      float v[64];
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + b * 128 + half * 64;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) tmem_ld16(ta + 16 * j, v + 16 * j);
+      tmem_wait_ld();
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar(B_HEMPTY + b));
+      const int r0 = row_begin + t * 128 + half * 64;  // first row of this slice
+      const uint32_t y0 = A.ybits[r0 >> 5], y1 = A.ybits[(r0 >> 5) + 1];
+      const int nvalid = max(0, min(64, row_end - r0));
+      float sum = 0.f, comp = 0.f;
+      uint32_t hi[32], lo[32];
+#pragma unroll
+      for (int j = 0; j < 64; j += 2) {
+        float rr[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int jj = j + e;
+          const uint32_t yb = ((jj < 32 ? y0 >> jj : y1 >> (jj - 32)) & 1u);
+          const float s = yb ? -1.f : 1.f;
+          const float u = s * v[jj];
+          const float ex = __expf(-fabsf(u));
+          const float onep = 1.f + ex;
+          const float sp = fmaxf(u, 0.f) + __logf(onep);
+          const float inv = __fdividef(1.f, onep);
+          const float sig = u >= 0.f ? inv : ex * inv;
+          const bool valid = jj < nvalid;
+          rr[e] = valid ? -s * sig : 0.f;
+          // Kahan: sum += -sp
+          const float term = valid ? -sp : 0.f;
+          const float yk = term - comp;
+          const float tk = sum + yk;
+          comp = (tk - sum) - yk;
+          sum = tk;
+        }
+        const float h0 = __bfloat162float(__float2bfloat16_rn(rr[0]));
+        const float h1 = __bfloat162float(__float2bfloat16_rn(rr[1]));
+        hi[j >> 1] = pack_bf16(h0, h1);
+        lo[j >> 1] = pack_bf16(rr[0] - h0, rr[1] - h1);
+      }
+      lp_acc += (double)sum;
+      if (t >= 1 && !mbar_wait(bar(B_REMPTY), (t - 1) & 1, abort)) { ok = false; break; }
+      // R tiles: row cl of the K-major SW128 layout, 8 chunks of 8 rows' values
+#pragma unroll
+      for (int ch = 0; ch < 8; ++ch) {
+        const int pc = (ch ^ (cl & 7)) * 16;
+        *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hi[4 * ch], hi[4 * ch + 1], hi[4 * ch + 2], hi[4 * ch + 3]);
+        *reinterpret_cast<uint4*>(rlo + pc) = make_uint4(lo[4 * ch], lo[4 * ch + 1], lo[4 * ch + 2], lo[4 * ch + 3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar(B_RFULL));
+    }
+    // G readout
+    if (ok && T > 0 && mbar_wait(bar(B_GDONE), 0, abort)) {
+      fence_after();
+      float g[64];
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + 256 + half * 64;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) tmem_ld16(ta + 16 * j, g + 16 * j);
+      tmem_wait_ld();
+      if (c < A.C) {
+        double* pg = A.part_g + ((size_t)split * A.C + c) * (A.K + 1);
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+          const int k = half * 64 + j;
+          if (k < A.K) pg[1 + k] = (double)g[j];
+          else if (k == A.K) pg[0] = (double)g[j];
+        }
+      }
+    } else if (T == 0 && c < A.C) {
+      double* pg = A.part_g + ((size_t)split * A.C + c) * (A.K + 1);
+      for (int k = half; k <= A.K; k += 2) pg[k] = 0.0;
+    }
+    lpx[half * 128 + cl] = lp_acc;
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+    if (half == 0 && c < A.C) A.part_lp[(size_t)split * A.C + c] = lpx[cl] + lpx[128 + cl];
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+  if (threadIdx.x == 0 && *abort) atomicExch(A.error, 1);
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled get_encode(std::string& err) {
+  static EncodeTiled fn = nullptr;
+  if (fn) return fn;
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+    err = "cuTensorMapEncodeTiled unavailable";
+    return nullptr;
+  }
+  fn = (EncodeTiled)p;
+  return fn;
+}
+
+int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+             std::string& err) {
+  EncodeTiled enc = get_encode(err);
+  if (!enc) return GNUTS_ERR_CUDA;
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {row_bytes};
+  cuuint32_t box[2] = {64, 128};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    err = "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r);
+    return GNUTS_ERR_CUDA;
+  }
+  return GNUTS_OK;
+}
+
+}  // namespace
+
+struct TcPlan {
+  CUtensorMap xmap, cmap;
+  TcArgs args;
+  dim3 grid;
+  uint16_t* coef = nullptr;
+  int* error = nullptr;
+  double* part_lp = nullptr;
+  double* part_g = nullptr;
+};
+
+bool tc_supported(const DevModel& M) { return M.kind == MK_LOGISTIC && M.Xtc && M.K + 1 <= XTC_LD; }
+
+int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uint16_t** coef_bf, int* S_out,
+              double** part_lp, double** part_g, std::string& err) {
+  if (!tc_supported(M)) {
+    err = "tensor-core gradient needs a logistic model with at most 103 predictors";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  TcPlan* p = new TcPlan();
+  const int Cpad = (C + 127) / 128 * 128;
+  const int ctiles = Cpad / 128;
+  // row splits: fill the 152 SMs with one CTA each
+  const int ntiles = (M.N + 127) / 128;
+  int S = std::max(1, 152 / ctiles);
+  S = std::min(S, ntiles);
+  const int tiles_per_split = (ntiles + S - 1) / S;
+  S = (ntiles + tiles_per_split - 1) / tiles_per_split;
+  auto fail = [&](cudaError_t e) {
+    err = std::string("CUDA error: ") + cudaGetErrorString(e);
+    tc_destroy(p);
+    return GNUTS_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&p->coef, sizeof(uint16_t) * 2 * Cpad * 128)) != cudaSuccess) return fail(e);
+  cudaMemset(p->coef, 0, sizeof(uint16_t) * 2 * Cpad * 128);
+  if ((e = cudaMalloc(&p->error, sizeof(int))) != cudaSuccess) return fail(e);
+  cudaMemset(p->error, 0, sizeof(int));
+  if ((e = cudaMalloc(&p->part_lp, sizeof(double) * S * C)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&p->part_g, sizeof(double) * S * C * (M.K + 1))) != cudaSuccess) return fail(e);
+  int rc = make_map(&p->xmap, M.Xtc, XTC_LD, (uint64_t)M.N, XTC_LD * 2, err);
+  if (!rc) rc = make_map(&p->cmap, p->coef, 128, (uint64_t)2 * Cpad, 256, err);
+  if (rc) {
+    tc_destroy(p);
+    return rc;
+  }
+  p->args = TcArgs{M.N, M.K, C, Cpad, tiles_per_split * 128, S, C, M.ybits, p->part_lp, p->part_g, done_count,
+                   p->error};
+  p->grid = dim3(ctiles, S);
+  if ((e = cudaFuncSetAttribute(k_glm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)) != cudaSuccess)
+    return fail(e);
+  *out = p;
+  *coef_bf = p->coef;
+  *S_out = S;
+  *part_lp = p->part_lp;
+  *part_g = p->part_g;
+  return GNUTS_OK;
+}
+
+void tc_destroy(TcPlan* p) {
+  if (!p) return;
+  cudaFree(p->coef);
+  cudaFree(p->error);
+  cudaFree(p->part_lp);
+  cudaFree(p->part_g);
+  delete p;
+}
+
+void tc_launch(const TcPlan* p, cudaStream_t stream) {
+  k_glm_tc<<<p->grid, NUM_THREADS, SMEM_BYTES, stream>>>(p->xmap, p->cmap, p->args);
+}
+
+int tc_error(const TcPlan* p) {
+  int h = 0;
+  cudaMemcpy(&h, p->error, sizeof(int), cudaMemcpyDeviceToHost);
+  return h;
+}
+
+}  // namespace gnuts

@@ -35,7 +35,13 @@ struct DevModel {
   const double* sigma;
   const double* scales;
   double scale_global, slab_scale, slab_df;
+  // tensor-core layout (logistic, K + 1 <= 128): X as BF16 rows of XTC_LD
+  // elements [x_1..x_K, 1, 0...] (the ones column carries the intercept) and
+  // y packed 32 rows per word
+  const uint16_t* Xtc;
+  const uint32_t* ybits;
 };
+constexpr int XTC_LD = 104;  // row stride in elements (208 B, a multiple of 16 B)
 
 struct Model {
   std::string id, name;
@@ -63,7 +69,7 @@ int run_transition(Model& m, int metric, const double* inv_metric, int n, const 
                    const double* p0, double eps, int max_depth, unsigned seed,
                    const unsigned* chain_ids, uint64_t* counters, double* q_out, double* stats,
                    std::string& err);
-int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, double* lp, double* grad,
+int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, int precision, double* lp, double* grad,
                       std::string& err);
 int run_write_array(Model& m, int n, const double* q, double* out, std::string& err);
 int upload(Model& m, std::string& err);

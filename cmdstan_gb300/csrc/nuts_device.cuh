@@ -43,7 +43,7 @@ struct Scal {
   unsigned w_nw, w_ib, w_tb, w_bw, w_counter, w_size, w_next, pad1;
   double wf_n;
   unsigned long long rng_n, irng_n;
-  long long n_grad;
+  long long n_grad, n_lf_total;
   unsigned long long t_start, t_warm, t_end;
   signed char stack[MAXREC];
   double r_lsw[MAXREC], r_lp[MAXREC], r_h[MAXREC];
@@ -495,6 +495,7 @@ struct Chain {
   // returns true if a gradient is requested
   __device__ bool end_transition() {
     const double accept = s.sum_metro / (double)s.n_leapfrog;
+    s.n_lf_total += s.n_leapfrog;
     __syncwarp();
     record(accept);
     const bool warm = s.iter < P.num_warmup;

@@ -19,6 +19,7 @@
 #include "internal.h"
 #include "nuts_device.cuh"
 #include "batched.cuh"
+#include "grad_tc.h"
 
 namespace gnuts {
 
@@ -143,6 +144,34 @@ __global__ void k_log_prob_grad(DevModel M, int n, const double* q, int jac, dou
   if (lane == 0) lp[warp] = v;
 }
 
+// FP32 and BF16 (round to nearest even) copies of the FP64 design matrix
+__global__ void k_derive_x(const double* X, size_t n, float* Xf, uint16_t* Xb) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float f = (float)X[i];
+    Xf[i] = f;
+    const uint32_t u = __float_as_uint(f);
+    Xb[i] = (uint16_t)((u + 0x7fffu + ((u >> 16) & 1u)) >> 16);
+  }
+}
+// tensor-core rows: [x_1..x_K, 1, 0 ...] in BF16, XTC_LD elements per row
+__global__ void k_derive_xtc(const uint16_t* Xb, size_t rows, int K, uint16_t* Xtc) {
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < rows; n += (size_t)gridDim.x * blockDim.x) {
+    for (int k = 0; k < XTC_LD; ++k)
+      Xtc[n * XTC_LD + k] = k < K ? Xb[n * K + k] : (k == K ? (uint16_t)0x3f80 : (uint16_t)0);
+  }
+}
+// y packed 32 rows per word (words beyond the data are zero)
+__global__ void k_pack_y(const int* y, size_t rows, size_t words, uint32_t* out) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x) {
+    uint32_t v = 0;
+    for (int b = 0; b < 32; ++b) {
+      const size_t n = w * 32 + b;
+      if (n < rows && y[n]) v |= 1u << b;
+    }
+    out[w] = v;
+  }
+}
+
 __global__ void k_write_array(DevModel M, int n, const double* q, double* out) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -196,6 +225,20 @@ bool use_rounds(const Model& m) {
   return batched_supported(m.dev) && m.dev.N >= 4096;
 }
 
+// the warp (fused) gradients hold a chain's coefficients in registers
+int check_warp_limits(const Model& m, std::string& err) {
+  if (use_rounds(m)) return GNUTS_OK;
+  if (m.dev.kind == MK_LOGISTIC && m.dev.K > 256) {
+    err = "logistic models with more than 256 predictors need N >= 4096 (batched gradient)";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  if (m.dev.kind == MK_HORSESHOE && m.dev.K > 1024) {
+    err = "horseshoe models support at most 1024 predictors";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  return GNUTS_OK;
+}
+
 }  // namespace
 
 int upload(Model& m, std::string& err) {
@@ -222,19 +265,33 @@ int upload(Model& m, std::string& err) {
     if ((rc = put(h.yr, sizeof(double) * n, (void**)&d.yr))) return rc;
   }
   if (h.X && xn) {
+    // only FP64 X crosses the bus; the FP32, BF16 and tensor-core copies are derived on the device
     if ((rc = put(h.X, sizeof(double) * xn, (void**)&d.X))) return rc;
-    std::vector<float> xf(xn);
-    std::vector<uint16_t> xb(xn);
-    for (size_t i = 0; i < xn; ++i) {
-      float f = (float)h.X[i];
-      xf[i] = f;
-      uint32_t u;
-      std::memcpy(&u, &f, 4);
-      uint32_t r = u + 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
-      xb[i] = (uint16_t)(r >> 16);
+    auto dev_alloc = [&](size_t bytes, void** dst) -> int {
+      cudaError_t e = cudaMalloc(dst, bytes);
+      if (e != cudaSuccess) { err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
+      m.device_allocs.push_back(*dst);
+      return GNUTS_OK;
+    };
+    if ((rc = dev_alloc(sizeof(float) * xn, (void**)&d.Xf))) return rc;
+    if ((rc = dev_alloc(sizeof(uint16_t) * xn, (void**)&d.Xb))) return rc;
+    const bool tc = h.kind == MK_LOGISTIC && h.K + 1 <= XTC_LD;
+    if (tc) {
+      if ((rc = dev_alloc(sizeof(uint16_t) * (size_t)h.N * XTC_LD, (void**)&d.Xtc))) return rc;
+      if ((rc = dev_alloc(sizeof(uint32_t) * (((size_t)h.N + 31) / 32 + 4), (void**)&d.ybits))) return rc;
     }
-    if ((rc = put(xf.data(), sizeof(float) * xn, (void**)&d.Xf))) return rc;
-    if ((rc = put(xb.data(), sizeof(uint16_t) * xn, (void**)&d.Xb))) return rc;
+    k_derive_x<<<std::min<size_t>(4096, (xn + 255) / 256), 256>>>(d.X, xn, const_cast<float*>(d.Xf),
+                                                                  const_cast<uint16_t*>(d.Xb));
+    if (tc) {
+      const size_t rows = (size_t)h.N;
+      k_derive_xtc<<<std::min<size_t>(4096, (rows + 255) / 256), 256>>>(d.Xb, rows, h.K,
+                                                                        const_cast<uint16_t*>(d.Xtc));
+      const size_t words = (rows + 31) / 32 + 4;
+      k_pack_y<<<std::min<size_t>(4096, (words + 255) / 256), 256>>>(d.yi, rows, words,
+                                                                     const_cast<uint32_t*>(d.ybits));
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { err = std::string("deriving X copies: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
   }
   if (h.group && (rc = put(h.group, sizeof(int) * h.N, (void**)&d.group))) return rc;
   if (h.gstart && (rc = put(h.gstart, sizeof(int) * (h.J + 1), (void**)&d.gstart))) return rc;
@@ -287,6 +344,8 @@ namespace {
 struct GradSetup {
   Arena ar;
   GradOut G{};
+  TcPlan* plan = nullptr;
+  ~GradSetup() { tc_destroy(plan); }
 };
 
 int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* done_count, std::string& err) {
@@ -296,6 +355,14 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   G.C = C;
   G.C_total = C;
   G.K = M.K;
+  G.done_count = done_count;
+  if (prec == GNUTS_PRECISION_MIXED && tc_supported(M)) {
+    int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g, err);
+    if (st) return st;
+    G.tc = gs.plan;
+    G.Cpad = (C + 127) / 128 * 128;
+    return GNUTS_OK;
+  }
   // row splits: enough CTAs to fill 152 SMs a few times over
   const int ctiles = (C + GLM_CT - 1) / GLM_CT;
   int S = std::max(1, (152 * 4 + ctiles - 1) / ctiles);
@@ -313,6 +380,10 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
 }
 
 void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
+  if (G.tc) {
+    tc_launch((const TcPlan*)G.tc, st);
+    return;
+  }
   dim3 grid((G.C + GLM_CT - 1) / GLM_CT, G.S);
   const bool small = M.K <= GLM_KC;
   if (G.prec == GNUTS_PRECISION_FP64) {
@@ -341,8 +412,12 @@ int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, d
   return GNUTS_OK;
 }
 
+struct RunStats {
+  double rounds = 0, grad_us = 0, advance_us = 0, device_ms = 0, launches = 0;
+};
+
 static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double per_chain_max, int refresh,
-                      gnuts_progress_fn progress, void* ctx, std::string& err) {
+                      gnuts_progress_fn progress, void* ctx, RunStats& stats, std::string& err) {
   const DevModel& M = m.dev;
   if (M.K > 1024) { err = "batched gradient supports at most 1024 predictors"; return GNUTS_ERR_ARGUMENT; }
   GradSetup gs;
@@ -356,16 +431,24 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   GN_CUDA(cudaDeviceSynchronize());  // k_init done
   k_stage<<<blocks, threads, 0, stream>>>(G, P, B, M);
   GN_CUDA(cudaGetLastError());
-  // capture ROUNDS x (gradient, advance) as one graph
+  // capture ROUNDS x (gradient, advance) as one graph; timing events bracket
+  // the two kernels of the graph's first round
   const int ROUNDS = 16;
+  cudaEvent_t tev[5];
+  for (auto& e : tev) GN_CUDA(cudaEventCreate(&e));
+  struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int i = 0; i < 5; ++i) cudaEventDestroy(e[i]); } } eg{tev};
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   GN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < ROUNDS; ++r) {
+    if (r == 0) GN_CUDA(cudaEventRecord(tev[0], stream));
     launch_glm(G, M, stream);
+    if (r == 0) GN_CUDA(cudaEventRecord(tev[1], stream));
     k_advance<<<blocks, threads, 0, stream>>>(P, B, M, G);
+    if (r == 0) GN_CUDA(cudaEventRecord(tev[2], stream));
   }
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
+  GN_CUDA(cudaEventRecord(tev[3], stream));
   GN_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   struct GraphGuard { cudaGraph_t g; cudaGraphExec_t e; ~GraphGuard() { cudaGraphExecDestroy(e); cudaGraphDestroy(g); } } gg{graph, exec};
   int* h_done = nullptr;
@@ -377,13 +460,28 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   GN_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
   const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
   int last_reported = -1;
+  long long graphs = 0;
+  double gsum = 0, asum = 0;
+  int nt = 0;
   for (long long l = 0; l < max_graphs; ++l) {
     const int b = (int)(l & 1);
     GN_CUDA(cudaGraphLaunch(exec, stream));
+    ++graphs;
     GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GN_CUDA(cudaEventRecord(ev[b], stream));
     if (l > 0) {
       GN_CUDA(cudaEventSynchronize(ev[b ^ 1]));
+      // the timing events hold the first round of the graph that just finished
+      // (sampled every 8th graph while chains are live)
+      if ((l & 7) == 1 && h_done[b ^ 1] < P.C) {
+        float g_ms = 0, a_ms = 0;
+        if (cudaEventElapsedTime(&g_ms, tev[0], tev[1]) == cudaSuccess &&
+            cudaEventElapsedTime(&a_ms, tev[1], tev[2]) == cudaSuccess) {
+          gsum += g_ms;
+          asum += a_ms;
+          ++nt;
+        }
+      }
       if (h_done[b ^ 1] >= P.C) break;
       if (progress && refresh > 0 && (l & 63) == 0) {
         Scal s0;
@@ -395,9 +493,21 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
       }
     }
   }
+  GN_CUDA(cudaEventRecord(tev[4], stream));
   GN_CUDA(cudaStreamSynchronize(stream));
+  if (gs.plan && tc_error(gs.plan)) {
+    err = "tensor-core gradient: a bounded pipeline wait ran out";
+    return GNUTS_ERR_TIMEOUT;
+  }
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
+  float total_ms = 0;
+  cudaEventElapsedTime(&total_ms, tev[3], tev[4]);
+  stats.rounds = (double)graphs * ROUNDS;
+  stats.grad_us = nt ? 1e3 * gsum / nt : 0;
+  stats.advance_us = nt ? 1e3 * asum / nt : 0;
+  stats.device_ms = total_ms;
+  stats.launches = (double)graphs * ROUNDS * 2 + 1;
   return GNUTS_OK;
 }
 
@@ -418,6 +528,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                          gnuts_progress_fn progress, void* ctx, std::string& err) {
   int st = upload(m, err);
   if (st) return st;
+  if ((st = check_warp_limits(m, err))) return st;
   const int C = a.num_chains, D = m.dev.D;
   Params P{};
   P.C = C;
@@ -509,16 +620,24 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   const double per_chain_max = (double)(a.num_warmup + a.num_samples) * (double)(1 << std::min(a.max_depth, 20)) +
                                8.0 * 1200.0 + 200.0;
   int done = 0;
+  RunStats stats;
   if (use_rounds(m) && !p0) {
-    st = run_rounds(m, P, B, a.precision, per_chain_max, a.refresh, progress, ctx, err);
+    st = run_rounds(m, P, B, a.precision, per_chain_max, a.refresh, progress, ctx, stats, err);
     if (st) return st;
     GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
   } else {
     const long long max_launches = (long long)(per_chain_max / P.grad_budget) + 16;
     int last_reported = -1;
+    cudaEvent_t f0, f1;
+    GN_CUDA(cudaEventCreate(&f0));
+    GN_CUDA(cudaEventCreate(&f1));
+    struct FEv { cudaEvent_t a, b; ~FEv() { cudaEventDestroy(a); cudaEventDestroy(b); } } fev{f0, f1};
+    GN_CUDA(cudaEventRecord(f0));
     for (long long l = 0; l < max_launches; ++l) {
       k_fused<<<blocks, threads>>>(P, B, m.dev, RB);
       GN_CUDA(cudaGetLastError());
+      stats.rounds += 1;
+      stats.launches += 1;
       GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
       if (progress && a.refresh > 0) {
         Scal s0;
@@ -531,7 +650,14 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       }
       if (done >= C) break;
     }
+    GN_CUDA(cudaEventRecord(f1));
+    GN_CUDA(cudaEventSynchronize(f1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, f0, f1);
+    stats.device_ms = ms;
+    stats.advance_us = stats.rounds > 0 ? 1e3 * ms / stats.rounds : 0;
   }
+  stats.launches += 1;  // k_init
   GN_CUDA(cudaDeviceSynchronize());
   if (done < C) {
     err = "sampler did not finish within its launch bound";
@@ -550,7 +676,16 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       if (out->warmup_seconds) out->warmup_seconds[c] = (double)(sc[c].t_warm - sc[c].t_start) * 1e-9;
       if (out->sampling_seconds) out->sampling_seconds[c] = (double)(sc[c].t_end - sc[c].t_warm) * 1e-9;
       if (out->n_grad) out->n_grad[c] = sc[c].n_grad;
+      if (out->n_leapfrog) out->n_leapfrog[c] = sc[c].n_lf_total;
       if (out->chain_status) out->chain_status[c] = sc[c].err ? (sc[c].err == CE_INIT ? GNUTS_ERR_INIT : GNUTS_ERR_SAMPLER) : GNUTS_OK;
+    }
+    if (out->timing) {
+      for (int i = 0; i < GNUTS_TIMING_FIELDS; ++i) out->timing[i] = 0;
+      out->timing[GNUTS_TIMING_ROUNDS] = stats.rounds;
+      out->timing[GNUTS_TIMING_GRAD_US] = stats.grad_us;
+      out->timing[GNUTS_TIMING_ADVANCE_US] = stats.advance_us;
+      out->timing[GNUTS_TIMING_DEVICE_MS] = stats.device_ms;
+      out->timing[GNUTS_TIMING_LAUNCHES] = stats.launches;
     }
   }
   if (counters)
@@ -603,7 +738,8 @@ int run_transition(Model& m, int metric, const double* inv_metric, int n, const 
   return GNUTS_OK;
 }
 
-int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, double* lp, double* grad, std::string& err) {
+int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, int precision, double* lp, double* grad,
+                      std::string& err) {
   int st = upload(m, err);
   if (st) return st;
   if (n <= 0) return GNUTS_OK;
@@ -614,8 +750,9 @@ int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, double* lp
   GN_CUDA(ar.alloc(&dg, (size_t)n * D));
   GN_CUDA(ar.alloc(&dl, n));
   GN_CUDA(cudaMemcpy(dq, q, sizeof(double) * n * D, cudaMemcpyHostToDevice));
-  if (batched_supported(m.dev) && m.dev.N >= 4096) {
-    st = batched_log_prob_grad(m.dev, n, dq, jacobian, dl, dg, GNUTS_PRECISION_FP64, err);
+  if (!use_rounds(m) && (st = check_warp_limits(m, err))) return st;
+  if (use_rounds(m)) {
+    st = batched_log_prob_grad(m.dev, n, dq, jacobian, dl, dg, precision, err);
     if (st) return st;
   } else {
     const int threads = 128, blocks = (n * 32 + threads - 1) / threads;

@@ -28,11 +28,45 @@ METRICS = {"diag_e": 0, "dense_e": 1, "unit_e": 2}
 EXPORTS = [
     "gnuts_model_create", "gnuts_model_create_json", "gnuts_model_destroy", "gnuts_model_dims",
     "gnuts_model_name", "gnuts_model_param_name", "gnuts_log_prob_grad", "gnuts_unconstrain",
-    "gnuts_write_array", "gnuts_sample_args_default", "gnuts_hmc_nuts_diag_e_adapt",
+    "gnuts_write_array", "gnuts_sample_args_default", "gnuts_log_prob_grad_precision", "gnuts_hmc_nuts_diag_e_adapt",
     "gnuts_hmc_nuts_dense_e_adapt", "gnuts_hmc_nuts_unit_e_adapt", "gnuts_hmc_nuts_diag_e",
     "gnuts_hmc_nuts_dense_e", "gnuts_hmc_nuts_unit_e", "gnuts_transition", "gnuts_last_error",
-    "gnuts_version",
+    "gnuts_version", "gnuts_summary", "gnuts_summary_columns",
 ]
+SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
+
+
+def summary(x, probs=(0.05, 0.5, 0.95)):
+    """stansummary statistics of one quantity; x is [chains, draws]."""
+    lib = load()
+    x = np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64)
+    p = np.ascontiguousarray(probs, dtype=np.float64)
+    out = np.zeros(7 + len(p))
+    _check(lib.gnuts_summary(_dp(x), x.shape[0], x.shape[1], x.shape[1], 1, _dp(p), len(p), _dp(out)))
+    return _summary_dict(out, probs)
+
+
+def _summary_dict(out, probs):
+    r = dict(zip(SUMMARY_FIELDS, out[:4]))
+    for i, pr in enumerate(probs):
+        r["q%g" % (100 * pr)] = out[4 + i]
+    n = len(probs)
+    r["ess_bulk"], r["ess_tail"], r["rhat"] = out[4 + n], out[5 + n], out[6 + n]
+    return r
+
+
+def summary_columns(draws, cols, probs=(0.05, 0.5, 0.95), threads=0):
+    """stansummary statistics of several columns of a [chains, draws, columns] array."""
+    lib = load()
+    d = np.ascontiguousarray(draws, dtype=np.float64)
+    C, n, K = d.shape
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    p = np.ascontiguousarray(probs, dtype=np.float64)
+    out = np.zeros((len(cols), 7 + len(p)))
+    _check(lib.gnuts_summary_columns(_dp(d), C, n, len(cols), n * K, K,
+                                     cols.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(p), len(p), threads,
+                                     _dp(out)))
+    return [_summary_dict(o, probs) for o in out]
 
 
 class GnutsError(RuntimeError):
@@ -62,7 +96,11 @@ class Var(ctypes.Structure):
 class Output(ctypes.Structure):
     _fields_ = [("draws", ctypes.c_void_p), ("stepsize", ctypes.c_void_p), ("inv_metric", ctypes.c_void_p),
                 ("warmup_seconds", ctypes.c_void_p), ("sampling_seconds", ctypes.c_void_p),
-                ("n_grad", ctypes.c_void_p), ("chain_status", ctypes.c_void_p)]
+                ("n_grad", ctypes.c_void_p), ("chain_status", ctypes.c_void_p), ("n_leapfrog", ctypes.c_void_p),
+                ("timing", ctypes.c_void_p)]
+
+
+TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "launches"]
 
 
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int)
@@ -88,6 +126,7 @@ def load():
     lib.gnuts_model_name.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     lib.gnuts_model_param_name.argtypes = [vp, ip, ip, ctypes.c_char_p, ctypes.c_size_t]
     lib.gnuts_log_prob_grad.argtypes = [vp, ip, dp, ip, dp, dp]
+    lib.gnuts_log_prob_grad_precision.argtypes = [vp, ip, dp, ip, ip, dp, dp]
     lib.gnuts_unconstrain.argtypes = [vp, dp, dp]
     lib.gnuts_write_array.argtypes = [vp, ip, dp, dp]
     lib.gnuts_sample_args_default.argtypes = [ctypes.POINTER(SampleArgs)]
@@ -102,6 +141,9 @@ def load():
                                      ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint64), dp, dp]
     lib.gnuts_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.gnuts_version.restype = ctypes.c_char_p
+    i64 = ctypes.c_int64
+    lib.gnuts_summary.argtypes = [dp, ip, ip, i64, i64, dp, ip, dp]
+    lib.gnuts_summary_columns.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, ip, dp]
     _lib = lib
     return lib
 
@@ -131,7 +173,8 @@ def default_args(**kw):
 class Fit:
     """Draws and adaptation results of one run (per chain)."""
 
-    def __init__(self, columns, draws, stepsize, inv_metric, warmup_seconds, sampling_seconds, n_grad, status):
+    def __init__(self, columns, draws, stepsize, inv_metric, warmup_seconds, sampling_seconds, n_grad, status,
+                 n_leapfrog=None, timing=None):
         self.columns = columns
         self.draws = draws                    # [chains, n_saved, 7 + num_constrained]
         self.stepsize = stepsize
@@ -140,6 +183,8 @@ class Fit:
         self.sampling_seconds = sampling_seconds
         self.n_grad = n_grad
         self.status = status
+        self.n_leapfrog = n_leapfrog          # per chain, warmup + sampling
+        self.timing = dict(zip(TIMING_FIELDS, timing)) if timing is not None else {}
 
     def column(self, name):
         return self.draws[:, :, self.columns.index(name)]
@@ -192,12 +237,16 @@ class Model:
             self._h = None
 
     # -- model_base surface
-    def log_prob_grad(self, q, jacobian=True):
+    def log_prob_grad(self, q, jacobian=True, precision=None):
         q = np.ascontiguousarray(np.atleast_2d(q), dtype=np.float64)
         n = q.shape[0]
         lp = np.zeros(n)
         g = np.zeros((n, self.dim))
-        _check(self._lib.gnuts_log_prob_grad(self._h, n, _dp(q), int(bool(jacobian)), _dp(lp), _dp(g)))
+        if precision is None:
+            _check(self._lib.gnuts_log_prob_grad(self._h, n, _dp(q), int(bool(jacobian)), _dp(lp), _dp(g)))
+        else:
+            _check(self._lib.gnuts_log_prob_grad_precision(self._h, n, _dp(q), int(bool(jacobian)), int(precision),
+                                                           _dp(lp), _dp(g)))
         return lp, g
 
     def unconstrain(self, constrained):
@@ -228,8 +277,10 @@ class Model:
         tw, ts = np.zeros(C), np.zeros(C)
         ng = np.zeros(C, dtype=np.int64)
         stt = np.zeros(C, dtype=np.int32)
+        nlf = np.zeros(C, dtype=np.int64)
+        tim = np.zeros(8)
         out = Output(draws.ctypes.data, eps.ctypes.data, minv.ctypes.data, tw.ctypes.data, ts.ctypes.data,
-                     ng.ctypes.data, stt.ctypes.data)
+                     ng.ctypes.data, stt.ctypes.data, nlf.ctypes.data, tim.ctypes.data)
         if inits is not None:
             inits = np.ascontiguousarray(np.broadcast_to(np.asarray(inits, dtype=np.float64), (C, D)))
         if inv_metric is not None:
@@ -248,7 +299,7 @@ class Model:
         _check(rc)
         if mk == 1:
             minv = minv.reshape(C, D, D)
-        return Fit(SAMPLER_COLUMNS + self.param_names, draws, eps, minv, tw, ts, ng, stt)
+        return Fit(SAMPLER_COLUMNS + self.param_names, draws, eps, minv, tw, ts, ng, stt, nlf, tim[:5])
 
     def transition(self, q0, p0, stepsize, inv_metric=None, metric="diag_e", max_depth=10, seed=0,
                    chain_ids=None, counters=None):

@@ -71,6 +71,11 @@ int gnuts_model_param_name(const gnuts_model* m, int index, int unconstrained, c
  * evaluated on the GPU.  q is n x num_params_r, grad is n x num_params_r. */
 int gnuts_log_prob_grad(const gnuts_model* m, int n, const double* q, int jacobian, double* lp,
                         double* grad);
+/* The same contract (command_helper.hpp:589-593) evaluated with the gradient
+ * precision the sampler uses for data-heavy models: GNUTS_PRECISION_MIXED
+ * selects the BF16-split tensor-core contraction, FP64 the CUDA-core one. */
+int gnuts_log_prob_grad_precision(const gnuts_model* m, int n, const double* q, int jacobian,
+                                  int precision, double* lp, double* grad);
 /* model_base::transform_inits / unconstrain_array (command_helper.hpp:334-351) */
 int gnuts_unconstrain(const gnuts_model* m, const double* constrained, double* unconstrained);
 /* model_base::write_array for n unconstrained points -> n x num_constrained */
@@ -108,7 +113,17 @@ typedef struct {
   double* sampling_seconds;  /* [num_chains] */
   int64_t* n_grad;           /* [num_chains] gradient evaluations incl. init and step-size search */
   int* chain_status;         /* [num_chains] GNUTS_OK or the chain's error code */
+  int64_t* n_leapfrog;       /* [num_chains] sum of n_leapfrog__ over all warmup + sampling iterations */
+  double* timing;            /* [GNUTS_TIMING_FIELDS] run telemetry, see GNUTS_TIMING_* */
 } gnuts_output;
+
+/* timing[] fields: device-side measurements of one run */
+#define GNUTS_TIMING_ROUNDS 0        /* gradient rounds (round mode) or fused launches */
+#define GNUTS_TIMING_GRAD_US 1       /* mean duration of the batched gradient kernel, us (CUDA events) */
+#define GNUTS_TIMING_ADVANCE_US 2    /* mean duration of the state-machine kernel, us (CUDA events) */
+#define GNUTS_TIMING_DEVICE_MS 3     /* device time from first to last launch, ms */
+#define GNUTS_TIMING_LAUNCHES 4      /* kernels launched by the run */
+#define GNUTS_TIMING_FIELDS 8
 
 /* Progress callback, called from the calling thread between device launches
  * (mirrors the `Iteration: k / n [pct%]` logger lines). May be NULL. */
@@ -146,6 +161,19 @@ int gnuts_hmc_nuts_unit_e(gnuts_model* m, const gnuts_sample_args* a, const doub
 int gnuts_transition(gnuts_model* m, int metric, const double* inv_metric, int n, const double* q0,
                      const double* p0, double stepsize, int max_depth, unsigned int seed,
                      const unsigned int* chain_ids, uint64_t* counters, double* q_out, double* stats);
+
+/* stansummary statistics of one quantity (stansummary_helper.hpp:397-428,
+ * chainset mean / mcse_mean / sd / med_abs_deviation / quantiles /
+ * split_rank_normalized_ess / split_rank_normalized_rhat).
+ * x[c * stride_chain + i * stride_iter] is draw i of chain c.
+ * out: mean, mcse, sd, mad, quantiles[n_probs], ess_bulk, ess_tail, rhat. */
+int gnuts_summary(const double* x, int n_chains, int n_iter, int64_t stride_chain, int64_t stride_iter,
+                  const double* probs, int n_probs, double* out);
+/* The same for n_cols quantities at once (threads over columns); out is
+ * n_cols x (7 + n_probs). */
+int gnuts_summary_columns(const double* draws, int n_chains, int n_iter, int n_cols, int64_t stride_chain,
+                          int64_t stride_iter, const int* cols, const double* probs, int n_probs,
+                          int n_threads, double* out);
 
 /* Message of the last failing call on this thread. */
 int gnuts_last_error(char* buf, size_t len);

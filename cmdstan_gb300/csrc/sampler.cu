@@ -242,6 +242,9 @@ int check_warp_limits(const Model& m, std::string& err) {
 }  // namespace
 
 int upload(Model& m, std::string& err) {
+  // every device entry point passes here: drop a stale non-sticky error left
+  // by an earlier runtime call so that launch checks report this call's errors
+  (void)cudaGetLastError();
   if (m.device >= 0) return GNUTS_OK;
   int rc = ensure_device(err);
   if (rc) return rc;
@@ -431,8 +434,9 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   GN_CUDA(cudaDeviceSynchronize());  // k_init done
   k_stage<<<blocks, threads, 0, stream>>>(G, P, B, M);
   GN_CUDA(cudaGetLastError());
-  // capture ROUNDS x (gradient, advance) as one graph; timing events bracket
-  // the two kernels of the graph's first round
+  // capture ROUNDS x (gradient, advance) as one graph.  Every 64th step of
+  // the loop runs one uncaptured round bracketed by events instead, which is
+  // where the per-kernel durations come from.
   const int ROUNDS = 16;
   cudaEvent_t tev[5];
   for (auto& e : tev) GN_CUDA(cudaEventCreate(&e));
@@ -441,11 +445,8 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   cudaGraphExec_t exec;
   GN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < ROUNDS; ++r) {
-    if (r == 0) GN_CUDA(cudaEventRecord(tev[0], stream));
     launch_glm(G, M, stream);
-    if (r == 0) GN_CUDA(cudaEventRecord(tev[1], stream));
     k_advance<<<blocks, threads, 0, stream>>>(P, B, M, G);
-    if (r == 0) GN_CUDA(cudaEventRecord(tev[2], stream));
   }
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
   GN_CUDA(cudaEventRecord(tev[3], stream));
@@ -460,27 +461,40 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   GN_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
   const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
   int last_reported = -1;
-  long long graphs = 0;
+  long long rounds = 0, launches = 0;
   double gsum = 0, asum = 0;
   int nt = 0;
-  for (long long l = 0; l < max_graphs; ++l) {
+  bool timed_pending = false;
+  for (long long l = 0; l < max_graphs * 2; ++l) {
     const int b = (int)(l & 1);
-    GN_CUDA(cudaGraphLaunch(exec, stream));
-    ++graphs;
+    const bool timed = (l & 63) == 5;
+    if (timed) {
+      GN_CUDA(cudaEventRecord(tev[0], stream));
+      launch_glm(G, M, stream);
+      GN_CUDA(cudaEventRecord(tev[1], stream));
+      k_advance<<<blocks, threads, 0, stream>>>(P, B, M, G);
+      GN_CUDA(cudaEventRecord(tev[2], stream));
+      rounds += 1;
+      launches += 2;
+    } else {
+      GN_CUDA(cudaGraphLaunch(exec, stream));
+      rounds += ROUNDS;
+      launches += 2 * ROUNDS;
+    }
     GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GN_CUDA(cudaEventRecord(ev[b], stream));
     if (l > 0) {
       GN_CUDA(cudaEventSynchronize(ev[b ^ 1]));
-      // the timing events hold the first round of the graph that just finished
-      // (sampled every 8th graph while chains are live)
-      if ((l & 7) == 1 && h_done[b ^ 1] < P.C) {
+      if (timed_pending) {
+        // the timed round was enqueued one step earlier and has completed
         float g_ms = 0, a_ms = 0;
-        if (cudaEventElapsedTime(&g_ms, tev[0], tev[1]) == cudaSuccess &&
+        if (h_done[b ^ 1] < P.C && cudaEventElapsedTime(&g_ms, tev[0], tev[1]) == cudaSuccess &&
             cudaEventElapsedTime(&a_ms, tev[1], tev[2]) == cudaSuccess) {
           gsum += g_ms;
           asum += a_ms;
           ++nt;
         }
+        timed_pending = false;
       }
       if (h_done[b ^ 1] >= P.C) break;
       if (progress && refresh > 0 && (l & 63) == 0) {
@@ -492,6 +506,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
         }
       }
     }
+    if (timed) timed_pending = true;
   }
   GN_CUDA(cudaEventRecord(tev[4], stream));
   GN_CUDA(cudaStreamSynchronize(stream));
@@ -503,11 +518,11 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   cudaEventDestroy(ev[1]);
   float total_ms = 0;
   cudaEventElapsedTime(&total_ms, tev[3], tev[4]);
-  stats.rounds = (double)graphs * ROUNDS;
+  stats.rounds = (double)rounds;
   stats.grad_us = nt ? 1e3 * gsum / nt : 0;
   stats.advance_us = nt ? 1e3 * asum / nt : 0;
   stats.device_ms = total_ms;
-  stats.launches = (double)graphs * ROUNDS * 2 + 1;
+  stats.launches = (double)launches + 1;  // + k_stage
   return GNUTS_OK;
 }
 

@@ -37,7 +37,33 @@ struct GradOut {
   void* tc;           // tensor-core plan (grad_tc.cu), null for the SIMT path
   uint16_t* coef_bf;  // tensor-core operand: [2][Cpad][128] BF16 hi / lo planes
   int Cpad;
+  double* gsum;       // [C][K+1] partials summed over the row splits (k_reduce_splits)
+  double* lpsum;      // [C]
 };
+
+// Sum the row-split partials: one thread per (chain, coefficient), fixed
+// order over splits (reproducible).  FP32 sums for the mixed path, whose
+// partials are FP32 tensor-memory accumulators; FP64 otherwise.  lp is summed
+// in FP64 in both.
+template <class Acc>
+__global__ void k_reduce_splits(GradOut G) {
+  if (G.done_count && *G.done_count >= G.C_total) return;
+  const int K1 = G.K + 1;
+  const size_t n = (size_t)G.C * K1;
+  const size_t stride = (size_t)G.C * K1;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n + G.C; i += (size_t)gridDim.x * blockDim.x) {
+    if (i < n) {
+      Acc t = 0;
+      for (int s = 0; s < G.S; ++s) t += (Acc)G.part_g[s * stride + i];
+      G.gsum[i] = (double)t;
+    } else {
+      const size_t c = i - n;
+      double t = 0;
+      for (int s = 0; s < G.S; ++s) t += G.part_lp[(size_t)s * G.C + c];
+      G.lpsum[c] = t;
+    }
+  }
+}
 
 inline bool batched_supported(const DevModel& M) {
   return M.kind == MK_LOGISTIC || M.kind == MK_HORSESHOE;
@@ -90,16 +116,14 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
 // sum the partials of chain c, add priors / Jacobian, write grad, return lp
 __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevModel& M, int c, const double* q,
                                                   double* g, int lane) {
-  const int K = M.K, S = G.S, C = G.C;
-  double lp = 0;
-  for (int s = lane; s < S; s += 32) lp += G.part_lp[(size_t)s * C + c];
-  lp = wsum(lp);
-  // likelihood gradient wrt (b0, beta) into g[0..K] (fixed summation order over s)
+  const int K = M.K;
+  double lp = G.lpsum[c];
+  const double* gs = G.gsum + (size_t)c * (K + 1);
+  // likelihood gradient wrt (b0, beta) -> g[0..K], priors added here
   if (M.kind == MK_LOGISTIC) {
     double pri = 0;
     for (int i = lane; i <= K; i += 32) {
-      double t = 0;
-      for (int s = 0; s < S; ++s) t += G.part_g[((size_t)s * C + c) * (K + 1) + i];
+      const double t = gs[i];
       double v = q[i];
       if (i == 0) {
         g[0] = t - v / 6.25;
@@ -117,8 +141,7 @@ __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevMod
   double c2 = ssl * ssl * caux;
   double pri = 0, glt = 0, glc = 0;
   for (int d = lane; d < K; d += 32) {
-    double t = 0;
-    for (int s = 0; s < S; ++s) t += G.part_g[((size_t)s * C + c) * (K + 1) + 1 + d];
+    const double t = gs[1 + d];
     double z = q[1 + d];
     double ll = q[K + 2 + d];
     double lam = exp(ll);
@@ -139,9 +162,7 @@ __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevMod
   glc = wsum(glc);
   double b0 = q[0];
   double ts = tau / sg;
-  double t0 = 0;
-  for (int s = lane; s < S; s += 32) t0 += G.part_g[((size_t)s * C + c) * (K + 1)];
-  t0 = wsum(t0);
+  const double t0 = gs[0];
   lp += pri - 0.5 * (b0 / 2.5) * (b0 / 2.5) - log1p(ts * ts) + (-0.5 * nu - 1.0) * lc - 0.5 * nu / caux + lt + lc;
   if (lane == 0) {
     g[0] = t0 - b0 / 6.25;

@@ -14,16 +14,18 @@
 // BF16 values).  Coefficients and residuals are split hi + lo in BF16, so
 // each contraction is two BF16 MMAs accumulated in FP32 TMEM (about 16
 // significant bits per operand).  softplus / inv_logit run in FP32; each
-// thread Kahan-sums its 64-row slice of lp in FP32 and adds it to an FP64
-// accumulator; the reduction over row splits is FP64 in the advance kernel.
+// thread sums its 32-row slice of lp in FP32 (four interleaved partial sums)
+// and adds it to an FP64 accumulator; the reduction over row splits is FP64
+// in the advance kernel.
 //
-// CTA = one 128-chain tile x one row split, 320 threads:
-//   warp 0      TMA producer: coefficient hi/lo tiles once, X row tiles
-//               (2-stage ring, 128 rows x 128 predictors, SWIZZLE_128B)
-//   warp 1      MMA issuer (one thread) + TMEM owner
-//   warps 2..9  epilogue: thread = (chain, half of the 128-row tile);
-//               reads its H slice from TMEM, writes R hi/lo into shared
-//               memory in the SW128 K-major layout GEMM2 reads
+// CTA = one 128-chain tile x one row split, 576 threads:
+//   warp 0       TMA producer: coefficient hi/lo tiles once, X row tiles
+//                (2-stage ring, 128 rows x 128 predictors, SWIZZLE_128B)
+//   warp 1       MMA issuer (one thread) + TMEM owner
+//   warps 2..17  epilogue: thread = (chain, 32-row slice of the tile), four
+//                warps per TMEM lane quadrant; reads its H slice from TMEM,
+//                writes R hi/lo into shared memory in the SW128 K-major
+//                layout GEMM2 reads; y of the split is staged as floats
 // TMEM: H double buffer (2 x 128 columns) + G (128 columns).
 // Every mbarrier wait is bounded; on expiry the kernel records an error,
 // drains what it issued and frees TMEM.
@@ -40,7 +42,9 @@ namespace {
 constexpr int TILE_BYTES = 128 * 128 * 2;   // [2 k-halves][128 rows][64] BF16
 constexpr int HALF_BYTES = TILE_BYTES / 2;  // one k-half: 128 rows x 128 B
 constexpr int NS = 2;
-constexpr int NUM_THREADS = 320;
+constexpr int EPI_WARPS = 16;                 // 4 per TMEM lane quadrant, 32 rows each
+constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
+constexpr int MAX_SPLIT_ROWS = 6144;          // y of a whole row split staged as floats
 constexpr int OFF_CHI = 0;
 constexpr int OFF_CLO = OFF_CHI + TILE_BYTES;
 constexpr int OFF_X = OFF_CLO + TILE_BYTES;
@@ -48,8 +52,9 @@ constexpr int OFF_RHI = OFF_X + NS * TILE_BYTES;
 constexpr int OFF_RLO = OFF_RHI + TILE_BYTES;
 constexpr int OFF_BAR = OFF_RLO + TILE_BYTES;  // 16 barriers
 constexpr int OFF_MISC = OFF_BAR + 16 * 8;     // tmem base, abort flag
-constexpr int OFF_LP = OFF_MISC + 16;          // [2][128] doubles
-constexpr int SMEM_USED = OFF_LP + 2 * 128 * 8;
+constexpr int OFF_LP = OFF_MISC + 16;          // [4][128] doubles
+constexpr int OFF_Y = OFF_LP + 4 * 128 * 8;    // [MAX_SPLIT_ROWS] floats
+constexpr int SMEM_USED = OFF_Y + MAX_SPLIT_ROWS * 4;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;   // alignment slack
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
@@ -137,6 +142,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// single-instruction approximations (SFU): 2^x, log2(x), 1/x
+__device__ __forceinline__ float ex2a(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2a(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcpa(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&v);
@@ -177,9 +199,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     mbar_init(bar(B_CFULL), 1);
     mbar_init(bar(B_HFULL), 1);
     mbar_init(bar(B_HFULL1), 1);
-    mbar_init(bar(B_HEMPTY), 8);
-    mbar_init(bar(B_HEMPTY1), 8);
-    mbar_init(bar(B_RFULL), 8);
+    mbar_init(bar(B_HEMPTY), EPI_WARPS);
+    mbar_init(bar(B_HEMPTY1), EPI_WARPS);
+    mbar_init(bar(B_RFULL), EPI_WARPS);
     mbar_init(bar(B_REMPTY), 1);
     mbar_init(bar(B_GDONE), 1);
     mbar_init(bar(B_DRAIN), 1);
@@ -278,97 +300,108 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       mbar_wait(bar(B_DRAIN), 0, &never);
     }
   } else {
-    // ---------------- epilogue: 8 warps, thread = (chain, row half)
-    const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
-    const int cl = q * 32 + lane;  // chain within the tile
+    // ---------------- epilogue: 16 warps, thread = (chain, 32-row slice of the tile)
+    const int q = warp & 3;             // TMEM lane quadrant (fixed by warp id % 4)
+    const int sub = (warp - 2) >> 2;    // rows [32 sub, 32 sub + 32) of each tile
+    const int cl = q * 32 + lane;       // chain within the tile
     const int c = c0 + cl;
+    const int et = threadIdx.x - 64;    // 0 .. 511
+    float* ys = (float*)(smem + OFF_Y);
+    // stage y of this row split as 0/1 floats (read back as warp-wide broadcasts)
+    for (int i = et; i < T * 128; i += 32 * EPI_WARPS) {
+      const int n = row_begin + i;
+      ys[i] = (n < row_end && ((A.ybits[n >> 5] >> (n & 31)) & 1u)) ? 1.f : 0.f;
+    }
+    asm volatile("bar.sync 1, 512;" ::: "memory");
     double lp_acc = 0.0;
-    uint8_t* rhi = smem + OFF_RHI + half * HALF_BYTES + cl * 128;
-    uint8_t* rlo = smem + OFF_RLO + half * HALF_BYTES + cl * 128;
+    const int kh = sub >> 1;            // k-half of the R tile this slice lands in
+    uint8_t* rhi = smem + OFF_RHI + kh * HALF_BYTES + cl * 128;
+    uint8_t* rlo = smem + OFF_RLO + kh * HALF_BYTES + cl * 128;
     bool ok = true;
     for (int t = 0; t < T && ok; ++t) {
       const int b = t & 1;
       if (!mbar_wait(bar(B_HFULL + b), (t >> 1) & 1, abort)) { ok = false; break; }
       fence_after();
-      float v[64];
-      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + b * 128 + half * 64;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) tmem_ld16(ta + 16 * j, v + 16 * j);
+      float v[32];
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + b * 128 + sub * 32;
+      tmem_ld16(ta, v);
+      tmem_ld16(ta + 16, v + 16);
       tmem_wait_ld();
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(bar(B_HEMPTY + b));
-      const int r0 = row_begin + t * 128 + half * 64;  // first row of this slice
-      const uint32_t y0 = A.ybits[r0 >> 5], y1 = A.ybits[(r0 >> 5) + 1];
-      const int nvalid = max(0, min(64, row_end - r0));
-      float sum = 0.f, comp = 0.f;
-      uint32_t hi[32], lo[32];
+      const int r0 = row_begin + t * 128 + sub * 32;
+      const float4* y4 = reinterpret_cast<const float4*>(ys + t * 128 + sub * 32);
+      const bool full = row_end - r0 >= 32;
+      float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+      uint32_t hi[16], lo[16];
 #pragma unroll
-      for (int j = 0; j < 64; j += 2) {
-        float rr[2];
+      for (int j4 = 0; j4 < 8; ++j4) {
+        const float4 yv = y4[j4];
+        const float yy[4] = {yv.x, yv.y, yv.z, yv.w};
+        float rr[4];
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          const int jj = j + e;
-          const uint32_t yb = ((jj < 32 ? y0 >> jj : y1 >> (jj - 32)) & 1u);
-          const float s = yb ? -1.f : 1.f;
-          const float u = s * v[jj];
-          const float ex = __expf(-fabsf(u));
-          const float onep = 1.f + ex;
-          const float sp = fmaxf(u, 0.f) + __logf(onep);
-          const float inv = __fdividef(1.f, onep);
-          const float sig = u >= 0.f ? inv : ex * inv;
-          const bool valid = jj < nvalid;
-          rr[e] = valid ? -s * sig : 0.f;
-          // Kahan: sum += -sp
-          const float term = valid ? -sp : 0.f;
-          const float yk = term - comp;
-          const float tk = sum + yk;
-          comp = (tk - sum) - yk;
-          sum = tk;
+        for (int e = 0; e < 4; ++e) {
+          const int j = 4 * j4 + e;
+          const float eta = v[j];
+          // e = exp(-|eta|); softplus(eta) = max(eta, 0) + log1p(e); inv_logit from the same e
+          const float ex = ex2a(-1.4426950408889634f * fabsf(eta));
+          const float d = 1.f + ex;
+          const float sp = fmaf(lg2a(d), 0.69314718055994531f, fmaxf(eta, 0.f));
+          const float inv = rcpa(d);
+          const float sig = eta >= 0.f ? inv : ex * inv;
+          float term = fmaf(yy[e], eta, -sp);  // y eta - softplus(eta)
+          float r = yy[e] - sig;               // y - inv_logit(eta)
+          if (!full && r0 + j >= row_end) { term = 0.f; r = 0.f; }
+          rr[e] = r;
+          if (e == 0) acc0 += term; else if (e == 1) acc1 += term; else if (e == 2) acc2 += term; else acc3 += term;
         }
-        const float h0 = __bfloat162float(__float2bfloat16_rn(rr[0]));
-        const float h1 = __bfloat162float(__float2bfloat16_rn(rr[1]));
-        hi[j >> 1] = pack_bf16(h0, h1);
-        lo[j >> 1] = pack_bf16(rr[0] - h0, rr[1] - h1);
-      }
-      lp_acc += (double)sum;
-      if (t >= 1 && !mbar_wait(bar(B_REMPTY), (t - 1) & 1, abort)) { ok = false; break; }
-      // R tiles: row cl of the K-major SW128 layout, 8 chunks of 8 rows' values
 #pragma unroll
-      for (int ch = 0; ch < 8; ++ch) {
-        const int pc = (ch ^ (cl & 7)) * 16;
-        *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hi[4 * ch], hi[4 * ch + 1], hi[4 * ch + 2], hi[4 * ch + 3]);
-        *reinterpret_cast<uint4*>(rlo + pc) = make_uint4(lo[4 * ch], lo[4 * ch + 1], lo[4 * ch + 2], lo[4 * ch + 3]);
+        for (int e = 0; e < 4; e += 2) {
+          const uint32_t h = pack_bf16(rr[e], rr[e + 1]);
+          const float h0 = __uint_as_float(h << 16), h1 = __uint_as_float(h & 0xffff0000u);
+          hi[2 * j4 + e / 2] = h;
+          lo[2 * j4 + e / 2] = pack_bf16(rr[e] - h0, rr[e + 1] - h1);
+        }
+      }
+      lp_acc += (double)((acc0 + acc1) + (acc2 + acc3));
+      if (t >= 1 && !mbar_wait(bar(B_REMPTY), (t - 1) & 1, abort)) { ok = false; break; }
+      // row cl of the K-major SW128 R tiles: 4 chunks of 8 rows' values
+#pragma unroll
+      for (int c4 = 0; c4 < 4; ++c4) {
+        const int pc = ((((sub & 1) * 4 + c4) ^ (cl & 7)) * 16);
+        *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hi[4 * c4], hi[4 * c4 + 1], hi[4 * c4 + 2], hi[4 * c4 + 3]);
+        *reinterpret_cast<uint4*>(rlo + pc) = make_uint4(lo[4 * c4], lo[4 * c4 + 1], lo[4 * c4 + 2], lo[4 * c4 + 3]);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(bar(B_RFULL));
     }
-    // G readout
+    // G readout: 32 predictor columns per thread
     if (ok && T > 0 && mbar_wait(bar(B_GDONE), 0, abort)) {
       fence_after();
-      float g[64];
-      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + 256 + half * 64;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) tmem_ld16(ta + 16 * j, g + 16 * j);
+      float g[32];
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + 256 + sub * 32;
+      tmem_ld16(ta, g);
+      tmem_ld16(ta + 16, g + 16);
       tmem_wait_ld();
       if (c < A.C) {
         double* pg = A.part_g + ((size_t)split * A.C + c) * (A.K + 1);
 #pragma unroll
-        for (int j = 0; j < 64; ++j) {
-          const int k = half * 64 + j;
+        for (int j = 0; j < 32; ++j) {
+          const int k = sub * 32 + j;
           if (k < A.K) pg[1 + k] = (double)g[j];
           else if (k == A.K) pg[0] = (double)g[j];
         }
       }
     } else if (T == 0 && c < A.C) {
       double* pg = A.part_g + ((size_t)split * A.C + c) * (A.K + 1);
-      for (int k = half; k <= A.K; k += 2) pg[k] = 0.0;
+      for (int k = sub; k <= A.K; k += 4) pg[k] = 0.0;
     }
-    lpx[half * 128 + cl] = lp_acc;
-    asm volatile("bar.sync 1, 256;" ::: "memory");
-    if (half == 0 && c < A.C) A.part_lp[(size_t)split * A.C + c] = lpx[cl] + lpx[128 + cl];
+    lpx[sub * 128 + cl] = lp_acc;
+    asm volatile("bar.sync 1, 512;" ::: "memory");
+    if (sub == 0 && c < A.C)
+      A.part_lp[(size_t)split * A.C + c] = (lpx[cl] + lpx[128 + cl]) + (lpx[256 + cl] + lpx[384 + cl]);
   }
   fence_before();
   __syncthreads();
@@ -442,7 +475,8 @@ int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uin
   const int ntiles = (M.N + 127) / 128;
   int S = std::max(1, 152 / ctiles);
   S = std::min(S, ntiles);
-  const int tiles_per_split = (ntiles + S - 1) / S;
+  // a split's y values are staged in shared memory: at most MAX_SPLIT_ROWS rows
+  const int tiles_per_split = std::min((ntiles + S - 1) / S, MAX_SPLIT_ROWS / 128);
   S = (ntiles + tiles_per_split - 1) / tiles_per_split;
   auto fail = [&](cudaError_t e) {
     err = std::string("CUDA error: ") + cudaGetErrorString(e);

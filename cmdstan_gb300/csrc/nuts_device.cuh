@@ -45,8 +45,9 @@ struct Scal {
   unsigned long long rng_n, irng_n;
   long long n_grad, n_lf_total;
   unsigned long long t_start, t_warm, t_end;
-  signed char stack[MAXREC];
-  double r_lsw[MAXREC], r_lp[MAXREC], r_h[MAXREC];
+  // pending left subtree per height: 5-bit record indices (31 = none),
+  // heights 0..11 in stk_lo, 12..17 in stk_hi
+  unsigned long long stk_lo, stk_hi;
 };
 
 struct Params {
@@ -60,12 +61,19 @@ struct Params {
   unsigned seed, id_base;
   double init_radius;
   int has_init, replay, n_saved, grad_budget;
+  int cache;          // chain vectors cached in shared memory during a launch
+  int cache_stride;   // doubles of shared memory per warp when cached
 };
+
+// vectors cached per chain (diag / unit metric also caches minv, wm, wm2)
+constexpr int NCACHE_VEC = 17;
+constexpr int NCACHE_VEC_DIAG = 20;
 
 struct Bufs {
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg;
   double *Tpb, *Tsb, *Tpe, *Tse, *Trho;
   double* rec;   // [C][R][7][ld]
+  double* recs;  // [C][R][3]: log-sum-weight, proposal lp, proposal energy of each record
   double* minv;  // diag/unit [C][ld]; dense [C][D][ld]
   double* chol;  // dense: transposed Cholesky factor Lt[k][i] = L[i][k], [C][D][ld]
   double *wm, *wm2, *tmp;
@@ -104,9 +112,12 @@ struct Chain {
   uint32_t chain_id;
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg, *Tpb, *Tsb, *Tpe, *Tse, *Trho;
   double *minv, *chol, *wm, *wm2, *tmp;
+  double* rsc;  // this chain's record scalars [R][3]
+  double* cache_base = nullptr;
 
   __device__ Chain(const Params& p, const Bufs& b, const DevModel& m, Scal& sc, int ci, int ln)
       : P(p), B(b), M(m), s(sc), c(ci), lane(ln), D(p.D) {
+    rsc = b.recs + (size_t)ci * p.R * 3;
     chain_id = p.id_base + (uint32_t)ci;
     size_t o = (size_t)ci * p.ld;
     Wq = b.Wq + o; Wp = b.Wp + o; Wg = b.Wg + o;
@@ -123,6 +134,62 @@ struct Chain {
   }
   __device__ double* rec(int r, int v) const {
     return B.rec + (((size_t)c * P.R + r) * 7 + v) * P.ld;
+  }
+  // record scalars: every lane writes the same value; a full-warp shuffle or
+  // __syncwarp separates reads from later writes of the same record
+  __device__ double& rlsw(int r) const { return rsc[r * 3 + 0]; }
+  __device__ double& rlp(int r) const { return rsc[r * 3 + 1]; }
+  __device__ double& rh(int r) const { return rsc[r * 3 + 2]; }
+  __device__ int stack_get(int h) const {
+    const unsigned long long w = h < 12 ? s.stk_lo : s.stk_hi;
+    return (int)((w >> (5 * (h < 12 ? h : h - 12))) & 31ull);
+  }
+  __device__ void stack_set(int h, int v) {
+    const int sh = 5 * (h < 12 ? h : h - 12);
+    const unsigned long long m = ~(31ull << sh), x = (unsigned long long)(v & 31) << sh;
+    if (h < 12) s.stk_lo = (s.stk_lo & m) | x;
+    else s.stk_hi = (s.stk_hi & m) | x;
+  }
+
+  // ---------------- shared-memory cache of the chain's vectors ----------------
+  // One launch loads the chain's working vectors into this warp's slice of
+  // shared memory (independent loads, all in flight at once) and writes them
+  // back at exit, so the state machine's dependent accesses stay on chip.
+  __device__ int cached_vectors() const { return P.metric == 1 ? NCACHE_VEC : NCACHE_VEC_DIAG; }
+  template <class F>
+  __device__ void for_each_cached(F f) {
+    double** v[NCACHE_VEC_DIAG] = {&Wq, &Wp, &Wg, &Fq, &Fp, &Fg, &Bq, &Bp, &Bg, &Sq,
+                                   &Sg, &Tpb, &Tsb, &Tpe, &Tse, &Trho, &tmp, &minv, &wm, &wm2};
+    const int n = cached_vectors();
+#pragma unroll
+    for (int i = 0; i < NCACHE_VEC_DIAG; ++i)
+      if (i < n) f(i, v[i]);
+  }
+  __device__ void cache_attach(double* base) {
+    cache_base = base;
+    double* g[NCACHE_VEC_DIAG];
+    for_each_cached([&](int i, double** p) {
+      g[i] = *p;
+      double* sm = base + (size_t)i * P.ld;
+      for (int d = lane; d < D; d += 32) sm[d] = g[i][d];
+      *p = sm;
+    });
+    double* sr = base + (size_t)cached_vectors() * P.ld;
+    for (int i = lane; i < P.R * 3; i += 32) sr[i] = rsc[i];
+    rsc = sr;
+    __syncwarp();
+  }
+  __device__ void cache_detach() {
+    __syncwarp();
+    const size_t o = (size_t)c * P.ld;
+    double* g[NCACHE_VEC_DIAG] = {B.Wq + o, B.Wp + o, B.Wg + o, B.Fq + o, B.Fp + o, B.Fg + o, B.Bq + o,
+                                  B.Bp + o, B.Bg + o, B.Sq + o, B.Sg + o, B.Tpb + o, B.Tsb + o, B.Tpe + o,
+                                  B.Tse + o, B.Trho + o, B.tmp + o, B.minv + o, B.wm + o, B.wm2 + o};
+    for_each_cached([&](int i, double** p) {
+      for (int d = lane; d < D; d += 32) g[i][d] = (*p)[d];
+    });
+    double* gr = B.recs + (size_t)c * P.R * 3;
+    for (int i = lane; i < P.R * 3; i += 32) gr[i] = rsc[i];
   }
 
   // ---------------- vector helpers ----------------
@@ -341,7 +408,8 @@ struct Chain {
     else load_W_from(Bq, Bp, Bg, s.B_lp);
     s.leaf = 0;
     s.free_mask = (1u << P.R) - 1u;
-    for (int h = 0; h < MAXREC; ++h) s.stack[h] = -1;
+    s.stk_lo = ~0ull;
+    s.stk_hi = ~0ull;
     begin_leapfrog(s.dir * s.eps);
     s.phase = PH_LEAF;
     return true;
@@ -350,12 +418,13 @@ struct Chain {
   // merge pending left subtree A (init) with the current subtree Bk (final);
   // result is left in A.  Returns the no-U-turn verdict.
   __device__ bool merge(int A, int Bk) {
-    double lsw_sub = lse(s.r_lsw[A], s.r_lsw[Bk]);
+    const double lswA = rlsw(A), lswB = rlsw(Bk);
+    double lsw_sub = lse(lswA, lswB);
     bool take;
-    if (s.r_lsw[Bk] > lsw_sub) {
+    if (lswB > lsw_sub) {
       take = true;
     } else {
-      double a = exp(s.r_lsw[Bk] - lsw_sub);
+      double a = exp(lswB - lsw_sub);
       take = uniform() < a;
     }
     double *Apb = rec(A, RV_PB), *Asb = rec(A, RV_SB), *Ape = rec(A, RV_PE), *Ase = rec(A, RV_SE),
@@ -379,8 +448,12 @@ struct Chain {
       if (take) { Aq[d] = Bq_[d]; Ag[d] = Bg_[d]; }
     }
     s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
-    if (take) { s.r_lp[A] = s.r_lp[Bk]; s.r_h[A] = s.r_h[Bk]; }
-    s.r_lsw[A] = lsw_sub;
+    if (take) {
+      const double lpB = rlp(Bk), hB = rh(Bk);
+      rlp(A) = lpB;
+      rh(A) = hB;
+    }
+    rlsw(A) = lsw_sub;
     __syncwarp();
     return (s1b > 0 && s1a > 0) && (s2b > 0 && s2a > 0) && (s3b > 0 && s3a > 0);
   }
@@ -402,15 +475,15 @@ struct Chain {
       pb[d] = p; pe[d] = p; se[d] = sb[d]; rho[d] = p;
       rq[d] = Wq[d]; rg[d] = Wg[d];
     }
-    s.r_lsw[r] = s.H0 - h;
-    s.r_lp[r] = s.W_lp;
-    s.r_h[r] = h;
+    rlsw(r) = s.H0 - h;
+    rlp(r) = s.W_lp;
+    rh(r) = h;
     __syncwarp();
     if (s.divergent) return end_transition();
     int cur = r, height = 0;
     while ((s.leaf >> height) & 1) {
-      int A = s.stack[height];
-      s.stack[height] = -1;
+      const int A = stack_get(height);
+      stack_set(height, 31);
       bool ok = merge(A, cur);
       free_rec(cur);
       cur = A;
@@ -418,7 +491,7 @@ struct Chain {
       if (!ok) return end_transition();
     }
     if (height == s.depth) return finish_doubling(cur);
-    s.stack[height] = (signed char)cur;
+    stack_set(height, cur);
     ++s.leaf;
     begin_leapfrog(e);
     return true;
@@ -432,10 +505,11 @@ struct Chain {
     }
     ++s.depth;
     bool take;
-    if (s.r_lsw[N] > s.lsw) {
+    const double lswN = rlsw(N);
+    if (lswN > s.lsw) {
       take = true;
     } else {
-      double a = exp(s.r_lsw[N] - s.lsw);
+      double a = exp(lswN - s.lsw);
       take = uniform() < a;
     }
     double *Npb = rec(N, RV_PB), *Nsb = rec(N, RV_SB), *Npe = rec(N, RV_PE), *Nse = rec(N, RV_SE),
@@ -443,10 +517,10 @@ struct Chain {
     if (take) {
       copy(Sq, Nq);
       copy(Sg, Ng);
-      s.S_lp = s.r_lp[N];
-      s.S_h = s.r_h[N];
+      s.S_lp = rlp(N);
+      s.S_h = rh(N);
     }
-    s.lsw = lse(s.lsw, s.r_lsw[N]);
+    s.lsw = lse(s.lsw, lswN);
     // In time order the trajectory is [init | final]: forward -> (T, N),
     // backward -> (N reversed, T).
     double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;
@@ -618,7 +692,7 @@ struct Chain {
   }
 
   // ---------------- driver ----------------
-  __device__ __noinline__ bool advance() {
+  __device__ __forceinline__ bool advance() {
     switch (s.phase) {
       case PH_INIT: {
         if (W_finite()) {

@@ -109,12 +109,15 @@ __global__ void __launch_bounds__(128) k_fused(Params P, Bufs B, DevModel M, Rep
   if (s.phase >= PH_DONE) return;
   Chain ch(P, B, M, s, warp, lane);
   if (RB.chain_ids) ch.chain_id = RB.chain_ids[warp];
+  extern __shared__ double gn_cache[];
+  if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
   for (int b = 0; b < P.grad_budget; ++b) {
     double lp = warp_log_prob_grad(M, ch.Wq, ch.Wg, 1, lane);
     __syncwarp();
     s.W_lp = lp;
     if (!ch.advance()) break;
   }
+  if (P.cache) ch.cache_detach();
   __syncwarp();
   if (lane == 0) B.sc[warp] = s;
 }
@@ -127,11 +130,14 @@ __global__ void __launch_bounds__(128) k_advance(Params P, Bufs B, DevModel M, G
   Scal s = B.sc[warp];
   if (s.phase >= PH_DONE) return;
   Chain ch(P, B, M, s, warp, lane);
+  extern __shared__ double gn_cache[];
+  if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
   // gather this chain's gradient from the batched kernel's partial sums
   s.W_lp = reduce_gradient(G, M, warp, ch.Wq, ch.Wg, lane);
   __syncwarp();
   bool more = ch.advance();
   if (more) stage_request(G, M, warp, ch.Wq, lane);
+  if (P.cache) ch.cache_detach();
   __syncwarp();
   if (lane == 0) B.sc[warp] = s;
 }
@@ -180,6 +186,9 @@ __global__ void k_write_array(DevModel M, int n, const double* q, double* out) {
 }
 
 // ---------------------------------------------------------------- host side
+// dynamic shared memory of k_fused / k_advance (128-thread blocks: 4 chains)
+static size_t cache_bytes(const Params& P) { return P.cache ? 4 * (size_t)P.cache_stride * sizeof(double) : 0; }
+
 namespace {
 
 struct Arena {
@@ -359,6 +368,8 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   G.C_total = C;
   G.K = M.K;
   G.done_count = done_count;
+  GN_CUDA(gs.ar.alloc(&G.gsum, (size_t)C * (M.K + 1)));
+  GN_CUDA(gs.ar.alloc(&G.lpsum, (size_t)C));
   if (prec == GNUTS_PRECISION_MIXED && tc_supported(M)) {
     int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g, err);
     if (st) return st;
@@ -382,20 +393,27 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   return GNUTS_OK;
 }
 
-void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
+// the batched contraction (tensor-core or SIMT) followed by the row-split
+// reduction; `mid` (optional) is recorded between the two
+void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st, cudaEvent_t mid = nullptr) {
   if (G.tc) {
     tc_launch((const TcPlan*)G.tc, st);
-    return;
-  }
-  dim3 grid((G.C + GLM_CT - 1) / GLM_CT, G.S);
-  const bool small = M.K <= GLM_KC;
-  if (G.prec == GNUTS_PRECISION_FP64) {
-    if (small) k_glm_simt<double, 1><<<grid, GLM_THREADS, 0, st>>>(G, M);
-    else k_glm_simt<double, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
   } else {
-    if (small) k_glm_simt<float, 1><<<grid, GLM_THREADS, 0, st>>>(G, M);
-    else k_glm_simt<float, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
+    dim3 grid((G.C + GLM_CT - 1) / GLM_CT, G.S);
+    const bool small = M.K <= GLM_KC;
+    if (G.prec == GNUTS_PRECISION_FP64) {
+      if (small) k_glm_simt<double, 1><<<grid, GLM_THREADS, 0, st>>>(G, M);
+      else k_glm_simt<double, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
+    } else {
+      if (small) k_glm_simt<float, 1><<<grid, GLM_THREADS, 0, st>>>(G, M);
+      else k_glm_simt<float, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
+    }
   }
+  if (mid) cudaEventRecord(mid, st);
+  const size_t n = (size_t)G.C * (M.K + 1) + G.C;
+  const int rb = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  if (G.prec == GNUTS_PRECISION_FP64) k_reduce_splits<double><<<rb, 256, 0, st>>>(G);
+  else k_reduce_splits<float><<<rb, 256, 0, st>>>(G);
 }
 
 }  // namespace
@@ -416,7 +434,7 @@ int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, d
 }
 
 struct RunStats {
-  double rounds = 0, grad_us = 0, advance_us = 0, device_ms = 0, launches = 0;
+  double rounds = 0, grad_us = 0, advance_us = 0, device_ms = 0, launches = 0, reduce_us = 0;
 };
 
 static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double per_chain_max, int refresh,
@@ -438,15 +456,15 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   // the loop runs one uncaptured round bracketed by events instead, which is
   // where the per-kernel durations come from.
   const int ROUNDS = 16;
-  cudaEvent_t tev[5];
+  cudaEvent_t tev[6];
   for (auto& e : tev) GN_CUDA(cudaEventCreate(&e));
-  struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int i = 0; i < 5; ++i) cudaEventDestroy(e[i]); } } eg{tev};
+  struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int i = 0; i < 6; ++i) cudaEventDestroy(e[i]); } } eg{tev};
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   GN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < ROUNDS; ++r) {
     launch_glm(G, M, stream);
-    k_advance<<<blocks, threads, 0, stream>>>(P, B, M, G);
+    k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
   }
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
   GN_CUDA(cudaEventRecord(tev[3], stream));
@@ -462,7 +480,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
   int last_reported = -1;
   long long rounds = 0, launches = 0;
-  double gsum = 0, asum = 0;
+  double gsum = 0, rsum = 0, asum = 0;
   int nt = 0;
   bool timed_pending = false;
   for (long long l = 0; l < max_graphs * 2; ++l) {
@@ -470,16 +488,16 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
     const bool timed = (l & 63) == 5;
     if (timed) {
       GN_CUDA(cudaEventRecord(tev[0], stream));
-      launch_glm(G, M, stream);
+      launch_glm(G, M, stream, tev[5]);
       GN_CUDA(cudaEventRecord(tev[1], stream));
-      k_advance<<<blocks, threads, 0, stream>>>(P, B, M, G);
+      k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
       GN_CUDA(cudaEventRecord(tev[2], stream));
       rounds += 1;
-      launches += 2;
+      launches += 3;
     } else {
       GN_CUDA(cudaGraphLaunch(exec, stream));
       rounds += ROUNDS;
-      launches += 2 * ROUNDS;
+      launches += 3 * ROUNDS;
     }
     GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GN_CUDA(cudaEventRecord(ev[b], stream));
@@ -487,10 +505,12 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
       GN_CUDA(cudaEventSynchronize(ev[b ^ 1]));
       if (timed_pending) {
         // the timed round was enqueued one step earlier and has completed
-        float g_ms = 0, a_ms = 0;
-        if (h_done[b ^ 1] < P.C && cudaEventElapsedTime(&g_ms, tev[0], tev[1]) == cudaSuccess &&
+        float g_ms = 0, r_ms = 0, a_ms = 0;
+        if (h_done[b ^ 1] < P.C && cudaEventElapsedTime(&g_ms, tev[0], tev[5]) == cudaSuccess &&
+            cudaEventElapsedTime(&r_ms, tev[5], tev[1]) == cudaSuccess &&
             cudaEventElapsedTime(&a_ms, tev[1], tev[2]) == cudaSuccess) {
           gsum += g_ms;
+          rsum += r_ms;
           asum += a_ms;
           ++nt;
         }
@@ -520,6 +540,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   cudaEventElapsedTime(&total_ms, tev[3], tev[4]);
   stats.rounds = (double)rounds;
   stats.grad_us = nt ? 1e3 * gsum / nt : 0;
+  stats.reduce_us = nt ? 1e3 * rsum / nt : 0;
   stats.advance_us = nt ? 1e3 * asum / nt : 0;
   stats.device_ms = total_ms;
   stats.launches = (double)launches + 1;  // + k_stage
@@ -575,6 +596,17 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   P.replay = p0 != nullptr;
   P.n_saved = (a.save_warmup ? (a.num_warmup + a.thin - 1) / a.thin : 0) + (a.num_samples + a.thin - 1) / a.thin;
   P.grad_budget = 2048;
+  // cache the chain vectors in shared memory when four chains fit in a block's budget
+  {
+    const int nvec = P.metric == 1 ? NCACHE_VEC : NCACHE_VEC_DIAG;
+    P.cache_stride = (nvec * P.ld + P.R * 3 + 1) & ~1;
+    const size_t bytes = 4 * (size_t)P.cache_stride * sizeof(double);
+    P.cache = bytes <= 160 * 1024;
+    if (P.cache) {
+      GN_CUDA(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      GN_CUDA(cudaFuncSetAttribute(k_advance, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    }
+  }
 
   Arena ar;
   Bufs B{};
@@ -584,6 +616,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                      &B.Tpb, &B.Tsb, &B.Tpe, &B.Tse, &B.Trho, &B.wm, &B.tmp};
   for (double** v : vecs) GN_CUDA(ar.alloc(v, vec));
   GN_CUDA(ar.alloc(&B.rec, vec * P.R * 7));
+  GN_CUDA(ar.alloc(&B.recs, (size_t)C * P.R * 3));
   GN_CUDA(ar.alloc(&B.minv, mat));
   GN_CUDA(ar.alloc(&B.wm2, mat));
   if (P.metric == 1) GN_CUDA(ar.alloc(&B.chol, mat));
@@ -649,7 +682,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     struct FEv { cudaEvent_t a, b; ~FEv() { cudaEventDestroy(a); cudaEventDestroy(b); } } fev{f0, f1};
     GN_CUDA(cudaEventRecord(f0));
     for (long long l = 0; l < max_launches; ++l) {
-      k_fused<<<blocks, threads>>>(P, B, m.dev, RB);
+      k_fused<<<blocks, threads, cache_bytes(P)>>>(P, B, m.dev, RB);
       GN_CUDA(cudaGetLastError());
       stats.rounds += 1;
       stats.launches += 1;
@@ -701,6 +734,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       out->timing[GNUTS_TIMING_ADVANCE_US] = stats.advance_us;
       out->timing[GNUTS_TIMING_DEVICE_MS] = stats.device_ms;
       out->timing[GNUTS_TIMING_LAUNCHES] = stats.launches;
+      out->timing[GNUTS_TIMING_REDUCE_US] = stats.reduce_us;
     }
   }
   if (counters)

@@ -100,7 +100,7 @@ class Output(ctypes.Structure):
                 ("timing", ctypes.c_void_p)]
 
 
-TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "launches"]
+TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "launches", "reduce_kernel_us"]
 
 
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int)
@@ -299,7 +299,8 @@ class Model:
         _check(rc)
         if mk == 1:
             minv = minv.reshape(C, D, D)
-        return Fit(SAMPLER_COLUMNS + self.param_names, draws, eps, minv, tw, ts, ng, stt, nlf, tim[:5])
+        return Fit(SAMPLER_COLUMNS + self.param_names, draws, eps, minv, tw, ts, ng, stt, nlf,
+                   tim[:len(TIMING_FIELDS)])
 
     def transition(self, q0, p0, stepsize, inv_metric=None, metric="diag_e", max_depth=10, seed=0,
                    chain_ids=None, counters=None):

@@ -123,6 +123,7 @@ typedef struct {
 #define GNUTS_TIMING_ADVANCE_US 2    /* mean duration of the state-machine kernel, us (CUDA events) */
 #define GNUTS_TIMING_DEVICE_MS 3     /* device time from first to last launch, ms */
 #define GNUTS_TIMING_LAUNCHES 4      /* kernels launched by the run */
+#define GNUTS_TIMING_REDUCE_US 5     /* mean duration of the row-split reduction kernel, us */
 #define GNUTS_TIMING_FIELDS 8
 
 /* Progress callback, called from the calling thread between device launches

@@ -540,6 +540,14 @@ int gnuts_log_prob_grad_precision(const gnuts_model* m, int n, const double* q, 
   return rc ? fail(rc, err) : GNUTS_OK;
 }
 
+int gnuts_log_prob_grad_noalloc(const gnuts_model* m, int n, const double* q_device, int jacobian, double* lp_device,
+                                double* grad_device) {
+  if (!m) return fail(GNUTS_ERR_ARGUMENT, "null model");
+  std::string err;
+  int rc = noalloc_log_prob_grad(*M(m), n, q_device, jacobian, lp_device, grad_device, err);
+  return rc ? fail(rc, err) : GNUTS_OK;
+}
+
 int gnuts_unconstrain(const gnuts_model* m, const double* c, double* q) {
   if (!m || !c || !q) return fail(GNUTS_ERR_ARGUMENT, "null argument");
   const DevModel& d = M(m)->dev;

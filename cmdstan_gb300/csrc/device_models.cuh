@@ -34,7 +34,7 @@ __device__ __forceinline__ double inv_logit(double a) {
 }
 
 // ---- bernoulli: theta ~ beta(1,1), y ~ bernoulli(theta), theta = inv_logit(u)
-__device__ __noinline__ double lpg_bernoulli(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_bernoulli(const DevModel& M, const double* q, double* g, int jac, int lane) {
   double u = q[0];
   double a = M.ysum + (jac ? 1.0 : 0.0), b = (M.N - M.ysum) + (jac ? 1.0 : 0.0);
   double th = inv_logit(u);
@@ -44,7 +44,7 @@ __device__ __noinline__ double lpg_bernoulli(const DevModel& M, const double* q,
 }
 
 // ---- normal: x_k ~ normal(0, s_k)
-__device__ __noinline__ double lpg_normal(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_normal(const DevModel& M, const double* q, double* g, int jac, int lane) {
   double lp = 0;
   for (int k = lane; k < M.K; k += 32) {
     double s = M.scales[k], x = q[k];
@@ -55,7 +55,7 @@ __device__ __noinline__ double lpg_normal(const DevModel& M, const double* q, do
 }
 
 // ---- funnel: v ~ normal(0,3), x_k ~ normal(0, exp(v/2))
-__device__ __noinline__ double lpg_funnel(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_funnel(const DevModel& M, const double* q, double* g, int jac, int lane) {
   double v = q[0];
   double ev = exp(-v);
   double lp = 0, gv = 0;
@@ -72,7 +72,7 @@ __device__ __noinline__ double lpg_funnel(const DevModel& M, const double* q, do
 }
 
 // ---- hier (eight schools, centered): [mu, theta_1..J, log tau]
-__device__ __noinline__ double lpg_hier(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_hier(const DevModel& M, const double* q, double* g, int jac, int lane) {
   const int J = M.J;
   double mu = q[0], lt = q[J + 1], tau = exp(lt);
   double lp = 0, gmu = 0, glt = 0;
@@ -101,7 +101,7 @@ __device__ __noinline__ double lpg_hier(const DevModel& M, const double* q, doub
 
 // ---- logistic (warp version; the batched tensor-core kernels live in grad_logistic.cu)
 // [alpha, beta_1..D]; lanes own beta elements, rows are walked sequentially.
-__device__ __noinline__ double lpg_logistic(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_logistic(const DevModel& M, const double* q, double* g, int jac, int lane) {
   const int D = M.K;  // predictors
   double alpha = q[0];
   double b[8], acc[8];
@@ -147,7 +147,7 @@ __device__ __noinline__ double lpg_logistic(const DevModel& M, const double* q, 
 }
 
 // ---- varint: [alpha_1..J, beta_1..K, log sigma_y, log tau]; rows sorted by group
-__device__ __noinline__ double lpg_varint(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_varint(const DevModel& M, const double* q, double* g, int jac, int lane) {
   const int J = M.J, K = M.K;
   const double* al = q;
   const double* be = q + J;
@@ -211,7 +211,7 @@ __device__ __noinline__ double lpg_varint(const DevModel& M, const double* q, do
 }
 
 // ---- horseshoe logistic (warp version): [beta0, z_1..D, log tau, log lambda_1..D, log caux]
-__device__ __noinline__ double lpg_horseshoe(const DevModel& M, const double* q, double* g, int jac, int lane) {
+static __device__ __noinline__ double lpg_horseshoe(const DevModel& M, const double* q, double* g, int jac, int lane) {
   const int D = M.K;
   double b0 = q[0], lt = q[D + 1], tau = exp(lt), lc = q[2 * D + 2], caux = exp(lc);
   const double nu = M.slab_df, ssl = M.slab_scale, sg = M.scale_global;

@@ -73,5 +73,7 @@ int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, int precis
                       std::string& err);
 int run_write_array(Model& m, int n, const double* q, double* out, std::string& err);
 int upload(Model& m, std::string& err);
+// noalloc.cu: the allocation-free batched gradient (device pointers)
+int noalloc_log_prob_grad(const Model& m, int n, const double* q, int jac, double* lp, double* g, std::string& err);
 
 }  // namespace gnuts

@@ -31,7 +31,7 @@ EXPORTS = [
     "gnuts_write_array", "gnuts_sample_args_default", "gnuts_log_prob_grad_precision", "gnuts_hmc_nuts_diag_e_adapt",
     "gnuts_hmc_nuts_dense_e_adapt", "gnuts_hmc_nuts_unit_e_adapt", "gnuts_hmc_nuts_diag_e",
     "gnuts_hmc_nuts_dense_e", "gnuts_hmc_nuts_unit_e", "gnuts_transition", "gnuts_last_error",
-    "gnuts_version", "gnuts_summary", "gnuts_summary_columns",
+    "gnuts_version", "gnuts_summary", "gnuts_summary_columns", "gnuts_log_prob_grad_noalloc",
 ]
 SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
 
@@ -127,6 +127,8 @@ def load():
     lib.gnuts_model_param_name.argtypes = [vp, ip, ip, ctypes.c_char_p, ctypes.c_size_t]
     lib.gnuts_log_prob_grad.argtypes = [vp, ip, dp, ip, dp, dp]
     lib.gnuts_log_prob_grad_precision.argtypes = [vp, ip, dp, ip, ip, dp, dp]
+    # device pointers (passed as integers)
+    lib.gnuts_log_prob_grad_noalloc.argtypes = [vp, ip, vp, ip, vp, vp]
     lib.gnuts_unconstrain.argtypes = [vp, dp, dp]
     lib.gnuts_write_array.argtypes = [vp, ip, dp, dp]
     lib.gnuts_sample_args_default.argtypes = [ctypes.POINTER(SampleArgs)]

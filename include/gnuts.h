@@ -176,6 +176,35 @@ int gnuts_summary_columns(const double* draws, int n_chains, int n_iter, int n_c
                           int64_t stride_iter, const int* cols, const double* probs, int n_probs,
                           int n_threads, double* out);
 
+/* Allocation-free gradient for callers that cannot allocate device memory.
+ * No counterpart in the reference: CmdStan computes gradients on the host.
+ * It exists for callers that run where cudaMalloc is not allowed -- code
+ * inside a memory pool or arena that owns all device memory, a host callback
+ * of another library, an allocator-free real-time loop -- but that can pass
+ * device buffers they already own.  Same contract as gnuts_log_prob_grad
+ * (lp and gradient, FP64), for the batched models "logistic" and "horseshoe",
+ * with q, lp and grad given as DEVICE pointers (n x num_params_r, n, n x
+ * num_params_r).  Its scratch (coefficients, row-split partial sums) lives in
+ * a fixed static device array of GNUTS_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until the process exits; it calls no cudaMalloc,
+ * cudaFree or allocating library routine.  Limits: n <= GNUTS_NOALLOC_MAX_POINTS
+ * and num_params_r of the coefficient row (predictors + 1) <= GNUTS_NOALLOC_MAX_COEF;
+ * larger requests fail with GNUTS_ERR_ARGUMENT.  The model's data must
+ * already be on the current device (any earlier device call on the handle,
+ * e.g. gnuts_log_prob_grad, uploads it).  The first call on each device looks
+ * up the scratch array's device address; make that first call before any
+ * stream capture.  All calls share the one scratch array and work on the
+ * legacy default stream, returning after the result is written: calls that
+ * overlap on the GPU (from several host threads) race. */
+#define GNUTS_NOALLOC_MAX_POINTS 64
+#define GNUTS_NOALLOC_MAX_COEF 128
+#define GNUTS_NOALLOC_MAX_SPLITS 32
+#define GNUTS_NOALLOC_SCRATCH_BYTES \
+  (8 * (GNUTS_NOALLOC_MAX_SPLITS * GNUTS_NOALLOC_MAX_POINTS * (GNUTS_NOALLOC_MAX_COEF + 1) + \
+        2 * GNUTS_NOALLOC_MAX_POINTS * GNUTS_NOALLOC_MAX_COEF + GNUTS_NOALLOC_MAX_POINTS))
+int gnuts_log_prob_grad_noalloc(const gnuts_model* m, int n, const double* q_device, int jacobian,
+                                double* lp_device, double* grad_device);
+
 /* Message of the last failing call on this thread. */
 int gnuts_last_error(char* buf, size_t len);
 /* Library version string, e.g. "gnuts 0.1 (sm_103a)". */

@@ -11,12 +11,15 @@
 // command_helper.hpp:589-593), done for 128 chains at once.
 //
 // Precision: X is BF16-exact (the workload's design matrix is defined on
-// BF16 values).  Coefficients and residuals are split hi + lo in BF16, so
-// each contraction is two BF16 MMAs accumulated in FP32 TMEM (about 16
-// significant bits per operand).  softplus / inv_logit run in FP32; each
-// thread sums its 32-row slice of lp in FP32 (four interleaved partial sums)
-// and adds it to an FP64 accumulator; the reduction over row splits is FP64
-// in the advance kernel.
+// BF16 values).  Coefficients are split hi + lo in BF16, so GEMM1 is two BF16
+// MMAs accumulated in FP32 TMEM (about 16 significant bits of each
+// coefficient: this is what keeps lp accurate).  Residuals enter GEMM2 in
+// BF16 (relative error 2^-9 per residual, about 1e-3 on a gradient
+// component); a gradient error leaves the leapfrog volume preserving and
+// reversible and lp is computed separately, so it does not bias the target.
+// softplus / inv_logit run in FP32; each thread sums its 32-row slice of lp
+// in FP32 (four interleaved partial sums) and adds it to an FP64
+// accumulator; the reduction over row splits is FP64.
 //
 // CTA = one 128-chain tile x one row split, 576 threads:
 //   warp 0       TMA producer: coefficient hi/lo tiles once, X row tiles
@@ -24,9 +27,11 @@
 //   warp 1       MMA issuer (one thread) + TMEM owner
 //   warps 2..17  epilogue: thread = (chain, 32-row slice of the tile), four
 //                warps per TMEM lane quadrant; reads its H slice from TMEM,
-//                writes R hi/lo into shared memory in the SW128 K-major
-//                layout GEMM2 reads; y of the split is staged as floats
-// TMEM: H double buffer (2 x 128 columns) + G (128 columns).
+//                writes R into one of two shared-memory buffers in the SW128
+//                K-major layout GEMM2 reads; y of the split is staged as floats
+// TMEM: H double buffer (2 x 128 columns) + G (128 columns).  With H and R
+// double-buffered, GEMM1 of tile t+1 and GEMM2 of tile t-1 run while the
+// epilogue works on tile t.
 // Every mbarrier wait is bounded; on expiry the kernel records an error,
 // drains what it issued and frees TMEM.
 #include <cuda.h>
@@ -48,9 +53,8 @@ constexpr int MAX_SPLIT_ROWS = 6144;          // y of a whole row split staged a
 constexpr int OFF_CHI = 0;
 constexpr int OFF_CLO = OFF_CHI + TILE_BYTES;
 constexpr int OFF_X = OFF_CLO + TILE_BYTES;
-constexpr int OFF_RHI = OFF_X + NS * TILE_BYTES;
-constexpr int OFF_RLO = OFF_RHI + TILE_BYTES;
-constexpr int OFF_BAR = OFF_RLO + TILE_BYTES;  // 16 barriers
+constexpr int OFF_R = OFF_X + NS * TILE_BYTES;  // 2 residual buffers (BF16)
+constexpr int OFF_BAR = OFF_R + 2 * TILE_BYTES;  // 16 barriers
 constexpr int OFF_MISC = OFF_BAR + 16 * 8;     // tmem base, abort flag
 constexpr int OFF_LP = OFF_MISC + 16;          // [4][128] doubles
 constexpr int OFF_Y = OFF_LP + 4 * 128 * 8;    // [MAX_SPLIT_ROWS] floats
@@ -60,8 +64,9 @@ constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
 // barrier indices
-enum { B_XFULL = 0, B_XEMPTY = NS, B_CFULL = 2 * NS, B_HFULL, B_HFULL1, B_HEMPTY, B_HEMPTY1, B_RFULL, B_REMPTY,
-       B_GDONE, B_DRAIN };
+enum { B_XFULL = 0, B_XEMPTY = NS, B_CFULL = 2 * NS, B_HFULL, B_HFULL1, B_HEMPTY, B_HEMPTY1, B_RFULL, B_RFULL1,
+       B_REMPTY, B_REMPTY1, B_GDONE, B_DRAIN };
+static_assert(B_DRAIN < 16, "barrier area holds 16 barriers");
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -202,7 +207,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     mbar_init(bar(B_HEMPTY), EPI_WARPS);
     mbar_init(bar(B_HEMPTY1), EPI_WARPS);
     mbar_init(bar(B_RFULL), EPI_WARPS);
+    mbar_init(bar(B_RFULL1), EPI_WARPS);
     mbar_init(bar(B_REMPTY), 1);
+    mbar_init(bar(B_REMPTY1), 1);
     mbar_init(bar(B_GDONE), 1);
     mbar_init(bar(B_DRAIN), 1);
     *abort = 0;
@@ -254,22 +261,21 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const uint32_t ID2 = idesc(false, true);   // A = R K-major, B = X MN-major
       const uint32_t tG = tmem + 256;
       bool ok = mbar_wait(bar(B_CFULL), 0, abort);
+      // GEMM2 of tile u: G += R(u) . X(u), R in residual buffer u & 1
       auto gemm2 = [&](int u) -> bool {
-        if (!mbar_wait(bar(B_RFULL), u & 1, abort)) return false;
+        const int rb = u & 1;
+        if (!mbar_wait(bar(B_RFULL + rb), (u >> 1) & 1, abort)) return false;
         fence_after();
         const uint32_t xs = sbase + OFF_X + (u % NS) * TILE_BYTES;
+        const uint32_t rs = sbase + OFF_R + rb * TILE_BYTES;
 #pragma unroll
-        for (int part = 0; part < 2; ++part) {
-          const uint32_t rs = sbase + (part ? OFF_RLO : OFF_RHI);
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            uint64_t a = sdesc(rs + (i >> 2) * HALF_BYTES + (i & 3) * 32, 0, 1024);
-            uint64_t b = sdesc(xs + i * 2048, HALF_BYTES, 1024);
-            mma(tG, a, b, ID2, (u > 0 || part > 0 || i > 0) ? 1u : 0u);
-          }
+        for (int i = 0; i < 8; ++i) {
+          uint64_t a = sdesc(rs + (i >> 2) * HALF_BYTES + (i & 3) * 32, 0, 1024);
+          uint64_t b = sdesc(xs + i * 2048, HALF_BYTES, 1024);
+          mma(tG, a, b, ID2, (u > 0 || i > 0) ? 1u : 0u);
         }
         mma_commit(bar(B_XEMPTY + u % NS));
-        mma_commit(bar(B_REMPTY));
+        mma_commit(bar(B_REMPTY + rb));
         return true;
       };
       int t = 0;
@@ -315,8 +321,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     asm volatile("bar.sync 1, 512;" ::: "memory");
     double lp_acc = 0.0;
     const int kh = sub >> 1;            // k-half of the R tile this slice lands in
-    uint8_t* rhi = smem + OFF_RHI + kh * HALF_BYTES + cl * 128;
-    uint8_t* rlo = smem + OFF_RLO + kh * HALF_BYTES + cl * 128;
+    uint8_t* rrow = smem + OFF_R + kh * HALF_BYTES + cl * 128;
     bool ok = true;
     for (int t = 0; t < T && ok; ++t) {
       const int b = t & 1;
@@ -332,50 +337,67 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       if (lane == 0) mbar_arrive(bar(B_HEMPTY + b));
       const int r0 = row_begin + t * 128 + sub * 32;
       const float4* y4 = reinterpret_cast<const float4*>(ys + t * 128 + sub * 32);
-      const bool full = row_end - r0 >= 32;
+      const int nvalid = row_end - r0;  // >= 32 on every tile but the last
       float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
-      uint32_t hi[16], lo[16];
+      uint32_t hi[16];
+      // per element: e = exp(-|eta|), softplus(eta) = max(eta, 0) + log1p(e),
+      // inv_logit(eta) from the same e; lp term y eta - softplus(eta), residual y - inv_logit(eta)
+#define GN_EPI_ELEMENT(J, Y, R, ACC)                                               \
+      {                                                                            \
+        const float eta = v[J];                                                    \
+        const float ex = ex2a(-1.4426950408889634f * fabsf(eta));                  \
+        const float d = 1.f + ex;                                                  \
+        const float sp = fmaf(lg2a(d), 0.69314718055994531f, fmaxf(eta, 0.f));     \
+        const float inv = rcpa(d);                                                 \
+        const float sig = (eta >= 0.f ? 1.f : ex) * inv;                           \
+        ACC += fmaf(Y, eta, -sp);                                                  \
+        R = Y - sig;                                                               \
+      }
+      if (nvalid >= 32) {
 #pragma unroll
-      for (int j4 = 0; j4 < 8; ++j4) {
-        const float4 yv = y4[j4];
-        const float yy[4] = {yv.x, yv.y, yv.z, yv.w};
-        float rr[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int j = 4 * j4 + e;
-          const float eta = v[j];
-          // e = exp(-|eta|); softplus(eta) = max(eta, 0) + log1p(e); inv_logit from the same e
-          const float ex = ex2a(-1.4426950408889634f * fabsf(eta));
-          const float d = 1.f + ex;
-          const float sp = fmaf(lg2a(d), 0.69314718055994531f, fmaxf(eta, 0.f));
-          const float inv = rcpa(d);
-          const float sig = eta >= 0.f ? inv : ex * inv;
-          float term = fmaf(yy[e], eta, -sp);  // y eta - softplus(eta)
-          float r = yy[e] - sig;               // y - inv_logit(eta)
-          if (!full && r0 + j >= row_end) { term = 0.f; r = 0.f; }
-          rr[e] = r;
-          if (e == 0) acc0 += term; else if (e == 1) acc1 += term; else if (e == 2) acc2 += term; else acc3 += term;
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 yv = y4[j4];
+          float r0v, r1v, r2v, r3v;
+          GN_EPI_ELEMENT(4 * j4 + 0, yv.x, r0v, acc0)
+          GN_EPI_ELEMENT(4 * j4 + 1, yv.y, r1v, acc1)
+          GN_EPI_ELEMENT(4 * j4 + 2, yv.z, r2v, acc2)
+          GN_EPI_ELEMENT(4 * j4 + 3, yv.w, r3v, acc3)
+          hi[2 * j4] = pack_bf16(r0v, r1v);
+          hi[2 * j4 + 1] = pack_bf16(r2v, r3v);
         }
+      } else {
+        // ragged last tile: rows at or past row_end contribute nothing
 #pragma unroll
-        for (int e = 0; e < 4; e += 2) {
-          const uint32_t h = pack_bf16(rr[e], rr[e + 1]);
-          const float h0 = __uint_as_float(h << 16), h1 = __uint_as_float(h & 0xffff0000u);
-          hi[2 * j4 + e / 2] = h;
-          lo[2 * j4 + e / 2] = pack_bf16(rr[e] - h0, rr[e + 1] - h1);
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 yv = y4[j4];
+          float rv[4];
+          const float yy[4] = {yv.x, yv.y, yv.z, yv.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            float a = 0.f, r;
+            GN_EPI_ELEMENT(4 * j4 + e, yy[e], r, a)
+            const bool valid = 4 * j4 + e < nvalid;
+            rv[e] = valid ? r : 0.f;
+            acc0 += valid ? a : 0.f;
+          }
+          hi[2 * j4] = pack_bf16(rv[0], rv[1]);
+          hi[2 * j4 + 1] = pack_bf16(rv[2], rv[3]);
         }
       }
+#undef GN_EPI_ELEMENT
       lp_acc += (double)((acc0 + acc1) + (acc2 + acc3));
-      if (t >= 1 && !mbar_wait(bar(B_REMPTY), (t - 1) & 1, abort)) { ok = false; break; }
-      // row cl of the K-major SW128 R tiles: 4 chunks of 8 rows' values
+      // residual buffer t & 1 is free once GEMM2 of tile t - 2 has completed
+      if (t >= 2 && !mbar_wait(bar(B_REMPTY + b), ((t >> 1) - 1) & 1, abort)) { ok = false; break; }
+      // row cl of the K-major SW128 residual tile: 4 chunks of 8 rows' values
+      uint8_t* rdst = rrow + b * TILE_BYTES;
 #pragma unroll
       for (int c4 = 0; c4 < 4; ++c4) {
         const int pc = ((((sub & 1) * 4 + c4) ^ (cl & 7)) * 16);
-        *reinterpret_cast<uint4*>(rhi + pc) = make_uint4(hi[4 * c4], hi[4 * c4 + 1], hi[4 * c4 + 2], hi[4 * c4 + 3]);
-        *reinterpret_cast<uint4*>(rlo + pc) = make_uint4(lo[4 * c4], lo[4 * c4 + 1], lo[4 * c4 + 2], lo[4 * c4 + 3]);
+        *reinterpret_cast<uint4*>(rdst + pc) = make_uint4(hi[4 * c4], hi[4 * c4 + 1], hi[4 * c4 + 2], hi[4 * c4 + 3]);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(bar(B_RFULL));
+      if (lane == 0) mbar_arrive(bar(B_RFULL + b));
     }
     // G readout: 32 predictor columns per thread
     if (ok && T > 0 && mbar_wait(bar(B_GDONE), 0, abort)) {

@@ -418,15 +418,22 @@ struct Chain {
   // merge pending left subtree A (init) with the current subtree Bk (final);
   // result is left in A.  Returns the no-U-turn verdict.
   __device__ bool merge(int A, int Bk) {
+    // record weights are finite here (a divergent leaf ends the transition
+    // before any merge).  One exp serves both the log-sum-exp and the
+    // probability w_B / (w_A + w_B) of taking B's proposal.
     const double lswA = rlsw(A), lswB = rlsw(Bk);
-    double lsw_sub = lse(lswA, lswB);
-    bool take;
-    if (lswB > lsw_sub) {
-      take = true;
+    const double x = lswB - lswA;
+    double lsw_sub, a;
+    if (x <= 0) {
+      const double e = exp(x);
+      lsw_sub = lswA + log1p(e);
+      a = e / (1.0 + e);
     } else {
-      double a = exp(lswB - lsw_sub);
-      take = uniform() < a;
+      const double e = exp(-x);
+      lsw_sub = lswB + log1p(e);
+      a = 1.0 / (1.0 + e);
     }
+    const bool take = uniform() < a;
     double *Apb = rec(A, RV_PB), *Asb = rec(A, RV_SB), *Ape = rec(A, RV_PE), *Ase = rec(A, RV_SE),
            *Arho = rec(A, RV_RHO), *Aq = rec(A, RV_Q), *Ag = rec(A, RV_G);
     double *Bpb = rec(Bk, RV_PB), *Bsb = rec(Bk, RV_SB), *Bpe = rec(Bk, RV_PE), *Bse = rec(Bk, RV_SE),
@@ -505,12 +512,17 @@ struct Chain {
     }
     ++s.depth;
     bool take;
+    // biased progressive sampling: a heavier new subtree is always taken
     const double lswN = rlsw(N);
-    if (lswN > s.lsw) {
+    const double x = lswN - s.lsw;
+    double lsw_new;
+    if (x > 0) {
       take = true;
+      lsw_new = lswN + log1p(exp(-x));
     } else {
-      double a = exp(lswN - s.lsw);
-      take = uniform() < a;
+      const double e = exp(x);
+      take = uniform() < e;
+      lsw_new = s.lsw + log1p(e);
     }
     double *Npb = rec(N, RV_PB), *Nsb = rec(N, RV_SB), *Npe = rec(N, RV_PE), *Nse = rec(N, RV_SE),
            *Nrho = rec(N, RV_RHO), *Nq = rec(N, RV_Q), *Ng = rec(N, RV_G);
@@ -520,7 +532,7 @@ struct Chain {
       s.S_lp = rlp(N);
       s.S_h = rh(N);
     }
-    s.lsw = lse(s.lsw, lswN);
+    s.lsw = lsw_new;
     // In time order the trajectory is [init | final]: forward -> (T, N),
     // backward -> (N reversed, T).
     double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;

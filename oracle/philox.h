@@ -12,9 +12,7 @@
  *   stream 0: sampler draws (jitter, momentum, direction, multinomial)
  *   stream 1: initialisation draws
  *   uniform   : one block -> ((o0<<32|o1) >> 11) * 2^-53          in [0,1)
- *   normal x2 : one block -> u1 = (((o0<<32|o1)>>11)+1) * 2^-53   in (0,1]
- *                            u2 = ((o2<<32|o3)>>11) * 2^-53
- *               Box-Muller: r = sqrt(-2 ln u1), (r cos 2pi u2, r sin 2pi u2)
+ *   normal x2 : one block -> FP32 Box-Muller from o0, o1 (orc_normal_from_block)
  *   momentum of D dims uses ceil(D/2) consecutive blocks; dims 2j, 2j+1
  *   take the pair of block j.
  */
@@ -22,6 +20,7 @@
 #define GNUTS_ORACLE_PHILOX_H
 #include <stdint.h>
 #include <math.h>
+#include <string.h>
 
 static inline void orc_philox_impl(const uint32_t c[4], const uint32_t k[2], uint32_t o[4]) {
   uint32_t x0 = c[0], x1 = c[1], x2 = c[2], x3 = c[3];
@@ -60,15 +59,64 @@ static inline double orc_next_uniform(orc_rng* g) {
   return (double)(x >> 11) * 0x1.0p-53;
 }
 
+/* FP32 Box-Muller from explicit correctly rounded steps (the oracle is built
+ * with -ffp-contract=off so that only the written fmaf calls fuse):
+ *   ln x  = e ln2 + s (2 + z (2/3 + z (2/5 + z (2/7 + z 2/9)))),
+ *           s = (m-1)/(m+1), z = s^2, x = m 2^e with m in [sqrt(1/2), sqrt(2))
+ *   sin a = a (1 - z/6 + z^2/120 - z^3/5040 + z^4/362880)        a in [0, pi/4]
+ *   cos a = 1 + z (-1/2 + z (1/24 + z (-1/720 + z (1/40320 - z/3628800))))
+ *   2 pi u2 = k pi/2 + phi, k = floor(4 u2), phi folded into [0, pi/4]. */
+static inline float orc_bm_log(float x) {
+  uint32_t bits;
+  memcpy(&bits, &x, 4);
+  int e = (int)(bits >> 23) - 127;
+  uint32_t mb = (bits & 0x7FFFFFu) | 0x3F800000u;
+  float m;
+  memcpy(&m, &mb, 4);
+  if (m > 1.41421356237309505f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float z = s * s;
+  float p = fmaf(z, 0.222222222222222222f, 0.285714285714285714f);
+  p = fmaf(z, p, 0.4f);
+  p = fmaf(z, p, 0.666666666666666667f);
+  p = fmaf(z, p, 2.0f);
+  return fmaf((float)e, 0.693147180559945309f, s * p);
+}
+static inline void orc_bm_quarter(float a, float* s, float* c) {
+  const float z = a * a;
+  float ps = fmaf(z, 2.75573192239858907e-6f, -1.98412698412698413e-4f);
+  ps = fmaf(z, ps, 8.33333333333333333e-3f);
+  ps = fmaf(z, ps, -0.166666666666666667f);
+  ps = fmaf(z, ps, 1.0f);
+  *s = a * ps;
+  float pc = fmaf(z, -2.75573192239858907e-7f, 2.48015873015873016e-5f);
+  pc = fmaf(z, pc, -1.38888888888888889e-3f);
+  pc = fmaf(z, pc, 4.16666666666666667e-2f);
+  pc = fmaf(z, pc, -0.5f);
+  *c = fmaf(z, pc, 1.0f);
+}
 static inline void orc_normal_from_block(const uint32_t o[4], double* z0, double* z1) {
-  uint64_t a = ((uint64_t)o[0] << 32) | o[1];
-  uint64_t b = ((uint64_t)o[2] << 32) | o[3];
-  double u1 = (double)((a >> 11) + 1) * 0x1.0p-53;
-  double u2 = (double)(b >> 11) * 0x1.0p-53;
-  double r = sqrt(-2.0 * log(u1));
-  double t = 6.283185307179586476925286766559 * u2;
-  *z0 = r * cos(t);
-  *z1 = r * sin(t);
+  const float u1 = (float)(((double)o[0] + 1.0) * 0x1.0p-32);
+  const float u2 = (float)(o[1] >> 8) * 0x1.0p-24f;
+  const float r = sqrtf(-2.0f * orc_bm_log(u1));
+  const float t = 4.0f * u2;
+  const float k = floorf(t);
+  const float f = t - k;
+  float s, c;
+  if (f <= 0.5f) orc_bm_quarter(f * 1.57079632679489662f, &s, &c);
+  else orc_bm_quarter((1.0f - f) * 1.57079632679489662f, &c, &s);
+  float cs, sn;
+  switch ((int)k) {
+    case 0: cs = c; sn = s; break;
+    case 1: cs = -s; sn = c; break;
+    case 2: cs = -c; sn = -s; break;
+    default: cs = s; sn = -c; break;
+  }
+  *z0 = (double)(r * cs);
+  *z1 = (double)(r * sn);
 }
 
 /* D standard normals, ceil(D/2) blocks */

@@ -308,9 +308,10 @@ def test_user_inits_and_init_zero():
 
 @pytest.mark.parametrize("N,D,n", [(10000, 100, 300), (4500, 37, 128), (8193, 103, 1)])
 def test_tensor_core_gradient_close_to_fp64(N, D, n):
-    """BF16 hi/lo split tensor-core contraction (tcgen05) vs the FP64 oracle.
-    Tolerances: lp relative 1e-4, gradient 2e-3 of its largest component, at
-    random points far from the mode (where the gradient is largest)."""
+    """Tensor-core contraction (tcgen05) vs the FP64 oracle: coefficients
+    split hi/lo in BF16 (lp), residuals in BF16 (gradient).  Tolerances: lp
+    relative 1e-4 and gradient 2e-3 of its largest component at random points
+    far from the mode; near the mode lp 1e-5 and gradient 3e-3."""
     data = workloads.logistic(seed=N, N=N, D=D)
     gm, om = _pair("logistic", data)
     rng = np.random.default_rng(N)
@@ -325,7 +326,7 @@ def test_tensor_core_gradient_close_to_fp64(N, D, n):
     lp, g = gm.log_prob_grad(qm, precision=gn.PRECISION_MIXED)
     olp, og = om.log_prob_grad(qm[0])
     assert abs(lp[0] - olp) <= 1e-5 * abs(olp)
-    assert np.max(np.abs(g[0] - og)) <= 1e-3 * np.max(np.abs(og))
+    assert np.max(np.abs(g[0] - og)) <= 3e-3 * np.max(np.abs(og))
 
 
 def test_tensor_core_sampler_moments_match_oracle():

@@ -275,7 +275,6 @@ def main():
     rhat_max = float(max(s["rhat"] for s in sm))
     step_s = last.timing["device_ms"] / 1e3
     grad_us = float(np.mean([f.timing["grad_kernel_us"] for f in fits]))
-    red_us = float(np.mean([f.timing["reduce_kernel_us"] for f in fits]))
     adv_us = float(np.mean([f.timing["advance_kernel_us"] for f in fits]))
     flops = 4.0 * N_ROWS * N_PRED * N_CHAINS
     achieved = flops / (grad_us * 1e-6) / 1e12
@@ -304,7 +303,7 @@ def main():
         "min_bulk_ess_per_s": ess_min / step_s, "min_bulk_ess": ess_min, "rhat_max": rhat_max,
         "sampler_device_s_per_step": dev_ms / 1e3 / args.steps,
         "leapfrogs_per_step": lf / args.steps,
-        "kernels_us": {"k_glm_tc": grad_us, "k_reduce_splits": red_us, "k_advance": adv_us},
+        "kernels_us": {"k_glm_tc": grad_us, "k_advance": adv_us},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": "%s bf16 sustained" % peak_kind,

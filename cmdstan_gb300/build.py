@@ -94,8 +94,9 @@ def build(verbose=False, jobs=None):
         _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
     cli_src = os.path.join(CLI, "gnuts_sample.cpp")
     exe = os.path.join(LIB, "gnuts-sample")
-    if os.path.exists(cli_src) and _newer(exe, [cli_src, so, os.path.join(INC, "gnuts.h")]):
-        _run(["g++"] + CXX_FLAGS + [cli_src, "-o", exe, "-L" + LIB, "-lgnuts", "-Wl,-rpath,$ORIGIN"])
+    cli_deps = [os.path.join(CLI, f) for f in os.listdir(CLI)] if os.path.isdir(CLI) else []
+    if os.path.exists(cli_src) and _newer(exe, cli_deps + [so, os.path.join(INC, "gnuts.h")]):
+        _run(["g++"] + CXX_FLAGS + ["-I" + CLI, cli_src, "-o", exe, "-L" + LIB, "-lgnuts", "-Wl,-rpath,$ORIGIN"])
     return so
 
 

@@ -37,32 +37,57 @@ struct GradOut {
   void* tc;           // tensor-core plan (grad_tc.cu), null for the SIMT path
   uint16_t* coef_bf;  // tensor-core operand: [2][Cpad][128] BF16 hi / lo planes
   int Cpad;
-  double* gsum;       // [C][K+1] partials summed over the row splits (k_reduce_splits)
-  double* lpsum;      // [C]
 };
 
-// Sum the row-split partials: one thread per (chain, coefficient), fixed
-// order over splits (reproducible).  FP32 sums for the mixed path, whose
-// partials are FP32 tensor-memory accumulators; FP64 otherwise.  lp is summed
-// in FP64 in both.
+// Sum the S row-split partials of chain c in a fixed order (s = 0, 1, ...):
+// FP32 sums for the mixed path, whose partials are FP32 tensor-memory
+// accumulators, FP64 otherwise.  Lane l owns coefficients l, l+32, ...; the
+// loads of 8 splits x SCH coefficients are issued together.  out[i] receives
+// the sum for coefficient i (i <= K).
+constexpr int SCH = 4;  // coefficients per lane per pass
 template <class Acc>
-__global__ void k_reduce_splits(GradOut G) {
-  if (G.done_count && *G.done_count >= G.C_total) return;
+__device__ __forceinline__ void sum_splits(const GradOut& G, int c, double* out, int lane) {
   const int K1 = G.K + 1;
-  const size_t n = (size_t)G.C * K1;
   const size_t stride = (size_t)G.C * K1;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n + G.C; i += (size_t)gridDim.x * blockDim.x) {
-    if (i < n) {
-      Acc t = 0;
-      for (int s = 0; s < G.S; ++s) t += (Acc)G.part_g[s * stride + i];
-      G.gsum[i] = (double)t;
-    } else {
-      const size_t c = i - n;
-      double t = 0;
-      for (int s = 0; s < G.S; ++s) t += G.part_lp[(size_t)s * G.C + c];
-      G.lpsum[c] = t;
+  const double* src = G.part_g + (size_t)c * K1;
+  for (int base = 0; base < K1; base += 32 * SCH) {
+    Acc acc[SCH];
+#pragma unroll
+    for (int j = 0; j < SCH; ++j) acc[j] = 0;
+    for (int s0 = 0; s0 < G.S; s0 += 8) {
+      double v[8][SCH];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int j = 0; j < SCH; ++j) {
+          const int i = base + lane + 32 * j;
+          v[u][j] = (s0 + u < G.S && i < K1) ? src[(size_t)(s0 + u) * stride + i] : 0.0;
+        }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int j = 0; j < SCH; ++j)
+          if (s0 + u < G.S) acc[j] += (Acc)v[u][j];
+    }
+#pragma unroll
+    for (int j = 0; j < SCH; ++j) {
+      const int i = base + lane + 32 * j;
+      if (i < K1) out[i] = (double)acc[j];
     }
   }
+}
+// lp partials of chain c summed in FP64, same order on every lane
+__device__ __forceinline__ double sum_split_lp(const GradOut& G, int c) {
+  double t = 0;
+  for (int s0 = 0; s0 < G.S; s0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = s0 + u < G.S ? G.part_lp[(size_t)(s0 + u) * G.C + c] : 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (s0 + u < G.S) t += v[u];
+  }
+  return t;
 }
 
 inline bool batched_supported(const DevModel& M) {
@@ -117,9 +142,12 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
 __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevModel& M, int c, const double* q,
                                                   double* g, int lane) {
   const int K = M.K;
-  double lp = G.lpsum[c];
-  const double* gs = G.gsum + (size_t)c * (K + 1);
-  // likelihood gradient wrt (b0, beta) -> g[0..K], priors added here
+  // likelihood gradient wrt (b0, beta) -> g[0..K]; priors added below
+  if (G.prec == GNUTS_PRECISION_FP64) sum_splits<double>(G, c, g, lane);
+  else sum_splits<float>(G, c, g, lane);
+  double lp = sum_split_lp(G, c);
+  __syncwarp();
+  const double* gs = g;
   if (M.kind == MK_LOGISTIC) {
     double pri = 0;
     for (int i = lane; i <= K; i += 32) {
@@ -162,10 +190,9 @@ __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevMod
   glc = wsum(glc);
   double b0 = q[0];
   double ts = tau / sg;
-  const double t0 = gs[0];
   lp += pri - 0.5 * (b0 / 2.5) * (b0 / 2.5) - log1p(ts * ts) + (-0.5 * nu - 1.0) * lc - 0.5 * nu / caux + lt + lc;
   if (lane == 0) {
-    g[0] = t0 - b0 / 6.25;
+    g[0] = gs[0] - b0 / 6.25;
     g[K + 1] = glt - 2.0 * ts * ts / (1.0 + ts * ts) + 1.0;
     g[2 * K + 2] = glc + (-0.5 * nu - 1.0) + 0.5 * nu / caux + 1.0;
   }

@@ -137,16 +137,12 @@ int noalloc_log_prob_grad(const Model& m, int n, const double* q, int jac, doubl
   G.part_g = scratch;                                   // S x n x (K+1)
   G.part_lp = G.part_g + (size_t)S * n * K1;            // S x n
   G.coef64 = scratch + (size_t)GNUTS_NOALLOC_MAX_SPLITS * GNUTS_NOALLOC_MAX_POINTS * (GNUTS_NOALLOC_MAX_COEF + 1);
-  G.gsum = G.coef64 + (size_t)GNUTS_NOALLOC_MAX_POINTS * GNUTS_NOALLOC_MAX_COEF;  // n x (K+1)
-  G.lpsum = G.gsum + (size_t)GNUTS_NOALLOC_MAX_POINTS * GNUTS_NOALLOC_MAX_COEF;   // n
   (void)cudaGetLastError();
   const int blocks = (n * 32 + 127) / 128;
   k_na_stage<<<blocks, 128>>>(G, M, n, q);
   dim3 grid((unsigned)ctiles, (unsigned)S);
   if (M.K <= GLM_KC) k_glm_simt<double, 1><<<grid, GLM_THREADS>>>(G, M);
   else k_glm_simt<double, 8><<<grid, GLM_THREADS>>>(G, M);
-  const size_t nred = (size_t)n * K1 + n;
-  k_reduce_splits<double><<<(unsigned)((nred + 255) / 256), 256>>>(G);
   k_na_finish<<<blocks, 128>>>(G, M, n, q, jac, lp, g);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);

@@ -68,6 +68,8 @@ struct Params {
 // vectors cached per chain (diag / unit metric also caches minv, wm, wm2)
 constexpr int NCACHE_VEC = 17;
 constexpr int NCACHE_VEC_DIAG = 20;
+// elements per lane whose loads are issued together in the record loops
+constexpr int VCH = 4;
 
 struct Bufs {
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg;
@@ -165,18 +167,25 @@ struct Chain {
     for (int i = 0; i < NCACHE_VEC_DIAG; ++i)
       if (i < n) f(i, v[i]);
   }
+  // global -> shared copies go through cp.async: no register round trip, all
+  // of them in flight at once, one wait at the end
+  static __device__ __forceinline__ void cp_async8(double* smem_dst, const double* gmem_src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem_dst)),
+                 "l"(gmem_src)
+                 : "memory");
+  }
   __device__ void cache_attach(double* base) {
     cache_base = base;
-    double* g[NCACHE_VEC_DIAG];
     for_each_cached([&](int i, double** p) {
-      g[i] = *p;
+      const double* gsrc = *p;
       double* sm = base + (size_t)i * P.ld;
-      for (int d = lane; d < D; d += 32) sm[d] = g[i][d];
+      for (int d = lane; d < D; d += 32) cp_async8(sm + d, gsrc + d);
       *p = sm;
     });
     double* sr = base + (size_t)cached_vectors() * P.ld;
-    for (int i = lane; i < P.R * 3; i += 32) sr[i] = rsc[i];
+    for (int i = lane; i < P.R * 3; i += 32) cp_async8(sr + i, rsc + i);
     rsc = sr;
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncwarp();
   }
   __device__ void cache_detach() {
@@ -193,8 +202,41 @@ struct Chain {
   }
 
   // ---------------- vector helpers ----------------
+  // chunks of 4 elements per lane: every load of a chunk is issued before its
+  // stores, so a copy costs one memory round trip per 128 elements
   __device__ void copy(double* dst, const double* src) const {
-    for (int d = lane; d < D; d += 32) dst[d] = src[d];
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double v[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        v[j] = d < D ? src[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        if (d < D) dst[d] = v[j];
+      }
+    }
+  }
+  __device__ void copy2(double* d1, const double* s1, double* d2, const double* s2) const {
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double v[VCH], w[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        v[j] = d < D ? s1[d] : 0.0;
+        w[j] = d < D ? s2[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        if (d < D) {
+          d1[d] = v[j];
+          d2[d] = w[j];
+        }
+      }
+    }
   }
   __device__ double dot(const double* a, const double* b) const {
     double t = 0;
@@ -439,21 +481,40 @@ struct Chain {
     double *Bpb = rec(Bk, RV_PB), *Bsb = rec(Bk, RV_SB), *Bpe = rec(Bk, RV_PE), *Bse = rec(Bk, RV_SE),
            *Brho = rec(Bk, RV_RHO), *Bq_ = rec(Bk, RV_Q), *Bg_ = rec(Bk, RV_G);
     double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;
-    for (int d = lane; d < D; d += 32) {
-      double rs = Arho[d] + Brho[d];
-      double e1 = Arho[d] + Bpb[d];
-      double e2 = Brho[d] + Ape[d];
-      s1a += Asb[d] * rs;
-      s1b += Bse[d] * rs;
-      s2a += Asb[d] * e1;
-      s2b += Bsb[d] * e1;
-      s3a += Ase[d] * e2;
-      s3b += Bse[d] * e2;
-      Arho[d] = rs;
-      Ape[d] = Bpe[d];
-      Ase[d] = Bse[d];
-      if (take) { Aq[d] = Bq_[d]; Ag[d] = Bg_[d]; }
+    // chunks of VCH elements per lane: all loads of a chunk are issued before
+    // any of its stores (the records live in global memory and the compiler
+    // cannot reorder loads across possibly aliasing stores).  Masked
+    // elements load 0 and add exact zeros to the sums.
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double arho[VCH], brho[VCH], bpb[VCH], ape[VCH], asb[VCH], bse[VCH], bsb[VCH], ase[VCH], bpe[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        const bool ok = d < D;
+        arho[j] = ok ? Arho[d] : 0.0; brho[j] = ok ? Brho[d] : 0.0; bpb[j] = ok ? Bpb[d] : 0.0;
+        ape[j] = ok ? Ape[d] : 0.0;   asb[j] = ok ? Asb[d] : 0.0;   bse[j] = ok ? Bse[d] : 0.0;
+        bsb[j] = ok ? Bsb[d] : 0.0;   ase[j] = ok ? Ase[d] : 0.0;   bpe[j] = ok ? Bpe[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const double rs = arho[j] + brho[j];
+        const double e1 = arho[j] + bpb[j];
+        const double e2 = brho[j] + ape[j];
+        s1a += asb[j] * rs;
+        s1b += bse[j] * rs;
+        s2a += asb[j] * e1;
+        s2b += bsb[j] * e1;
+        s3a += ase[j] * e2;
+        s3b += bse[j] * e2;
+        const int d = base + lane + 32 * j;
+        if (d < D) {
+          Arho[d] = rs;
+          Ape[d] = bpe[j];
+          Ase[d] = bse[j];
+        }
+      }
     }
+    if (take) copy2(Aq, Bq_, Ag, Bg_);
     s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
     if (take) {
       const double lpB = rlp(Bk), hB = rh(Bk);
@@ -472,14 +533,26 @@ struct Chain {
     int r = alloc_rec();
     double *pb = rec(r, RV_PB), *sb = rec(r, RV_SB), *pe = rec(r, RV_PE), *se = rec(r, RV_SE),
            *rho = rec(r, RV_RHO), *rq = rec(r, RV_Q), *rg = rec(r, RV_G);
-    dtau(sb, Wp);
-    double h = kinetic(Wp, sb) - s.W_lp;
+    // p_sharp = minv p is formed in registers and stored to both ends of the
+    // new leaf record (the dense metric needs the warp-wide product first)
+    double kin = 0;
+    if (P.metric == 1) {
+      dtau(tmp, Wp);
+      for (int d = lane; d < D; d += 32) kin += Wp[d] * tmp[d];
+    } else {
+      for (int d = lane; d < D; d += 32) {
+        const double p = Wp[d];
+        kin += p * (P.metric == 0 ? minv[d] * p : p);
+      }
+    }
+    double h = 0.5 * wsum(kin) - s.W_lp;
     if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
     if (h - s.H0 > 1000.0) s.divergent = 1;
     s.sum_metro += (s.H0 - h > 0) ? 1.0 : exp(s.H0 - h);
     for (int d = lane; d < D; d += 32) {
-      double p = Wp[d];
-      pb[d] = p; pe[d] = p; se[d] = sb[d]; rho[d] = p;
+      const double p = Wp[d];
+      const double ps = P.metric == 1 ? tmp[d] : (P.metric == 0 ? minv[d] * p : p);
+      pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
       rq[d] = Wq[d]; rg[d] = Wg[d];
     }
     rlsw(r) = s.H0 - h;
@@ -527,8 +600,7 @@ struct Chain {
     double *Npb = rec(N, RV_PB), *Nsb = rec(N, RV_SB), *Npe = rec(N, RV_PE), *Nse = rec(N, RV_SE),
            *Nrho = rec(N, RV_RHO), *Nq = rec(N, RV_Q), *Ng = rec(N, RV_G);
     if (take) {
-      copy(Sq, Nq);
-      copy(Sg, Ng);
+      copy2(Sq, Nq, Sg, Ng);
       s.S_lp = rlp(N);
       s.S_h = rh(N);
     }
@@ -536,25 +608,38 @@ struct Chain {
     // In time order the trajectory is [init | final]: forward -> (T, N),
     // backward -> (N reversed, T).
     double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;
-    if (s.dir > 0) {
-      for (int d = lane; d < D; d += 32) {
-        double rs = Trho[d] + Nrho[d];
-        double e1 = Trho[d] + Npb[d];
-        double e2 = Nrho[d] + Tpe[d];
-        s1a += Tsb[d] * rs; s1b += Nse[d] * rs;
-        s2a += Tsb[d] * e1; s2b += Nsb[d] * e1;
-        s3a += Tse[d] * e2; s3b += Nse[d] * e2;
-        Trho[d] = rs; Tpe[d] = Npe[d]; Tse[d] = Nse[d];
+    // loads of a chunk ahead of its stores, as in merge
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double trho[VCH], tpb[VCH], tpe[VCH], tsb[VCH], tse[VCH], nrho[VCH], npb[VCH], npe[VCH], nsb[VCH], nse[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        const bool ok = d < D;
+        trho[j] = ok ? Trho[d] : 0.0; tpb[j] = ok ? Tpb[d] : 0.0; tpe[j] = ok ? Tpe[d] : 0.0;
+        tsb[j] = ok ? Tsb[d] : 0.0;   tse[j] = ok ? Tse[d] : 0.0; nrho[j] = ok ? Nrho[d] : 0.0;
+        npb[j] = ok ? Npb[d] : 0.0;   npe[j] = ok ? Npe[d] : 0.0; nsb[j] = ok ? Nsb[d] : 0.0;
+        nse[j] = ok ? Nse[d] : 0.0;
       }
-    } else {
-      for (int d = lane; d < D; d += 32) {
-        double rs = Nrho[d] + Trho[d];
-        double e1 = Nrho[d] + Tpb[d];
-        double e2 = Trho[d] + Npb[d];
-        s1a += Nse[d] * rs; s1b += Tse[d] * rs;
-        s2a += Nse[d] * e1; s2b += Tsb[d] * e1;
-        s3a += Nsb[d] * e2; s3b += Tse[d] * e2;
-        Trho[d] = rs; Tpb[d] = Npe[d]; Tsb[d] = Nse[d];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        if (s.dir > 0) {
+          const double rs = trho[j] + nrho[j];
+          const double e1 = trho[j] + npb[j];
+          const double e2 = nrho[j] + tpe[j];
+          s1a += tsb[j] * rs; s1b += nse[j] * rs;
+          s2a += tsb[j] * e1; s2b += nsb[j] * e1;
+          s3a += tse[j] * e2; s3b += nse[j] * e2;
+          if (d < D) { Trho[d] = rs; Tpe[d] = npe[j]; Tse[d] = nse[j]; }
+        } else {
+          const double rs = nrho[j] + trho[j];
+          const double e1 = nrho[j] + tpb[j];
+          const double e2 = trho[j] + npb[j];
+          s1a += nse[j] * rs; s1b += tse[j] * rs;
+          s2a += nse[j] * e1; s2b += tsb[j] * e1;
+          s3a += nsb[j] * e2; s3b += tse[j] * e2;
+          if (d < D) { Trho[d] = rs; Tpb[d] = npe[j]; Tsb[d] = nse[j]; }
+        }
       }
     }
     s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);

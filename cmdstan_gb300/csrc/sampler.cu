@@ -368,8 +368,6 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   G.C_total = C;
   G.K = M.K;
   G.done_count = done_count;
-  GN_CUDA(gs.ar.alloc(&G.gsum, (size_t)C * (M.K + 1)));
-  GN_CUDA(gs.ar.alloc(&G.lpsum, (size_t)C));
   if (prec == GNUTS_PRECISION_MIXED && tc_supported(M)) {
     int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g, err);
     if (st) return st;
@@ -393,9 +391,9 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   return GNUTS_OK;
 }
 
-// the batched contraction (tensor-core or SIMT) followed by the row-split
-// reduction; `mid` (optional) is recorded between the two
-void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st, cudaEvent_t mid = nullptr) {
+// the batched contraction (tensor-core or SIMT); its row-split partials are
+// summed by the consumer (reduce_gradient, inside the state-machine kernel)
+void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
   if (G.tc) {
     tc_launch((const TcPlan*)G.tc, st);
   } else {
@@ -409,11 +407,6 @@ void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st, cudaEvent_
       else k_glm_simt<float, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
     }
   }
-  if (mid) cudaEventRecord(mid, st);
-  const size_t n = (size_t)G.C * (M.K + 1) + G.C;
-  const int rb = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-  if (G.prec == GNUTS_PRECISION_FP64) k_reduce_splits<double><<<rb, 256, 0, st>>>(G);
-  else k_reduce_splits<float><<<rb, 256, 0, st>>>(G);
 }
 
 }  // namespace
@@ -480,7 +473,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
   int last_reported = -1;
   long long rounds = 0, launches = 0;
-  double gsum = 0, rsum = 0, asum = 0;
+  double gsum = 0, asum = 0;
   int nt = 0;
   bool timed_pending = false;
   for (long long l = 0; l < max_graphs * 2; ++l) {
@@ -488,16 +481,16 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
     const bool timed = (l & 63) == 5;
     if (timed) {
       GN_CUDA(cudaEventRecord(tev[0], stream));
-      launch_glm(G, M, stream, tev[5]);
+      launch_glm(G, M, stream);
       GN_CUDA(cudaEventRecord(tev[1], stream));
       k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
       GN_CUDA(cudaEventRecord(tev[2], stream));
       rounds += 1;
-      launches += 3;
+      launches += 2;
     } else {
       GN_CUDA(cudaGraphLaunch(exec, stream));
       rounds += ROUNDS;
-      launches += 3 * ROUNDS;
+      launches += 2 * ROUNDS;
     }
     GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GN_CUDA(cudaEventRecord(ev[b], stream));
@@ -505,12 +498,10 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
       GN_CUDA(cudaEventSynchronize(ev[b ^ 1]));
       if (timed_pending) {
         // the timed round was enqueued one step earlier and has completed
-        float g_ms = 0, r_ms = 0, a_ms = 0;
-        if (h_done[b ^ 1] < P.C && cudaEventElapsedTime(&g_ms, tev[0], tev[5]) == cudaSuccess &&
-            cudaEventElapsedTime(&r_ms, tev[5], tev[1]) == cudaSuccess &&
+        float g_ms = 0, a_ms = 0;
+        if (h_done[b ^ 1] < P.C && cudaEventElapsedTime(&g_ms, tev[0], tev[1]) == cudaSuccess &&
             cudaEventElapsedTime(&a_ms, tev[1], tev[2]) == cudaSuccess) {
           gsum += g_ms;
-          rsum += r_ms;
           asum += a_ms;
           ++nt;
         }
@@ -540,7 +531,6 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   cudaEventElapsedTime(&total_ms, tev[3], tev[4]);
   stats.rounds = (double)rounds;
   stats.grad_us = nt ? 1e3 * gsum / nt : 0;
-  stats.reduce_us = nt ? 1e3 * rsum / nt : 0;
   stats.advance_us = nt ? 1e3 * asum / nt : 0;
   stats.device_ms = total_ms;
   stats.launches = (double)launches + 1;  // + k_stage

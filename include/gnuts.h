@@ -123,7 +123,7 @@ typedef struct {
 #define GNUTS_TIMING_ADVANCE_US 2    /* mean duration of the state-machine kernel, us (CUDA events) */
 #define GNUTS_TIMING_DEVICE_MS 3     /* device time from first to last launch, ms */
 #define GNUTS_TIMING_LAUNCHES 4      /* kernels launched by the run */
-#define GNUTS_TIMING_REDUCE_US 5     /* mean duration of the row-split reduction kernel, us */
+#define GNUTS_TIMING_REDUCE_US 5     /* 0: the row-split sums run inside the state-machine kernel */
 #define GNUTS_TIMING_FIELDS 8
 
 /* Progress callback, called from the calling thread between device launches
@@ -201,7 +201,7 @@ int gnuts_summary_columns(const double* draws, int n_chains, int n_iter, int n_c
 #define GNUTS_NOALLOC_MAX_SPLITS 32
 #define GNUTS_NOALLOC_SCRATCH_BYTES \
   (8 * (GNUTS_NOALLOC_MAX_SPLITS * GNUTS_NOALLOC_MAX_POINTS * (GNUTS_NOALLOC_MAX_COEF + 1) + \
-        2 * GNUTS_NOALLOC_MAX_POINTS * GNUTS_NOALLOC_MAX_COEF + GNUTS_NOALLOC_MAX_POINTS))
+        GNUTS_NOALLOC_MAX_POINTS * GNUTS_NOALLOC_MAX_COEF))
 int gnuts_log_prob_grad_noalloc(const gnuts_model* m, int n, const double* q_device, int jacobian,
                                 double* lp_device, double* grad_device);
 

@@ -3,7 +3,8 @@
 Reads the Stan CSV fixtures that the reference's stansummary / diagnose tests
 use (src/test/interface/example_output/*.csv under the reference checkout
 given as argv[1]) and writes, for each, a JSON file with the column names,
-the draw matrix and the adaptation block.  The expected summary numbers are
+the draw matrix and the comment blocks (config header, adaptation block,
+elapsed-time trailer).  The expected summary numbers are
 the literal goldens of src/test/interface/stansummary_test.cpp (:481-495,
 :622-637) and are written into the tests themselves.
 
@@ -15,13 +16,20 @@ import sys
 
 
 def parse_stan_csv(path):
-    names, rows, adapt = None, [], []
+    """Column names, draws, and the comment blocks: the config header before
+    the column names, the adaptation block between the names and the first
+    draw, and the trailer after the last draw."""
+    names, rows, config, adapt, trailer = None, [], [], [], []
     with open(path) as f:
         for line in f:
             line = line.rstrip("\n")
             if line.startswith("#"):
-                if names is not None and not rows:
+                if names is None:
+                    config.append(line)
+                elif not rows:
                     adapt.append(line)
+                else:
+                    trailer.append(line)
                 continue
             if not line.strip():
                 continue
@@ -29,19 +37,21 @@ def parse_stan_csv(path):
                 names = line.split(",")
                 continue
             rows.append([float(v) for v in line.split(",")])
-    return names, rows, adapt
+    return names, rows, config, adapt, trailer
 
 
 def main(ref):
     here = os.path.dirname(os.path.abspath(__file__))
     src = os.path.join(ref, "src", "test", "interface", "example_output")
     for stem in ("bernoulli_chain_1", "eight_schools_output"):
-        names, rows, adapt = parse_stan_csv(os.path.join(src, stem + ".csv"))
+        names, rows, config, adapt, trailer = parse_stan_csv(os.path.join(src, stem + ".csv"))
         out = {
             "source": "src/test/interface/example_output/%s.csv" % stem,
             "names": names,
             "draws": rows,
+            "config": config,
             "adaptation": adapt,
+            "trailer": trailer,
         }
         with open(os.path.join(here, stem + ".json"), "w") as f:
             json.dump(out, f, separators=(",", ":"))

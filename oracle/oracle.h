@@ -111,6 +111,19 @@ double orc_rhat(const double* x, int n_chains, int n_draws);
 void orc_summary(const double* x, int n_chains, int n_draws, const double* probs, int n_probs,
                  double* out);
 
+
+/* ---- affine-coupling flow (flow.cpp; no counterpart in the reference) ----
+ * theta layout and the map are defined at the top of flow.cpp. */
+long orc_flow_num_params(int d, int L, int H);
+void orc_flow_mask(int d, int L, int H, int l, int* out);
+double orc_flow_forward(int d, int L, int H, double clamp, const double* theta, const double* z, double* x);
+double orc_flow_inverse(int d, int L, int H, double clamp, const double* theta, const double* x, double* z);
+double orc_flow_log_prob_grad(const orc_model* m, int L, int H, double clamp, const double* theta,
+                              const double* z, int jacobian, double* grad_z, double* thbar, double* x_out,
+                              double* lp_x_out);
+void orc_adam(long n, double* theta, double* m, double* v, const double* g, int t, double lr, double b1,
+              double b2, double eps);
+
 #ifdef __cplusplus
 }
 #endif

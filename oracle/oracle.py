@@ -77,6 +77,16 @@ def load():
         L.orc_uniform.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]
         L.orc_uniform.restype = ctypes.c_double
         L.orc_normal_pair.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, _dp]
+        L.orc_flow_num_params.argtypes = [ctypes.c_int] * 3
+        L.orc_flow_num_params.restype = ctypes.c_long
+        L.orc_flow_mask.argtypes = [ctypes.c_int] * 4 + [_ip]
+        for f in ("orc_flow_forward", "orc_flow_inverse"):
+            getattr(L, f).argtypes = [ctypes.c_int] * 3 + [ctypes.c_double, _dp, _dp, _dp]
+            getattr(L, f).restype = ctypes.c_double
+        L.orc_flow_log_prob_grad.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp,
+                                             ctypes.c_int, _dp, _dp, _dp, _dp]
+        L.orc_flow_log_prob_grad.restype = ctypes.c_double
+        L.orc_adam.argtypes = [ctypes.c_long, _dp, _dp, _dp, _dp, ctypes.c_int] + [ctypes.c_double] * 4
         _lib = L
     return _lib
 
@@ -212,3 +222,53 @@ def philox(ctr, key):
     o = (ctypes.c_uint32 * 4)()
     L.orc_philox4x32_10(c, k, o)
     return list(o)
+
+
+class OracleFlow:
+    """FP64 twin of the affine-coupling flow (flow.cpp): theta is a flat
+    parameter vector in the layout documented there."""
+
+    def __init__(self, d, layers=8, hidden=128, clamp=4.0):
+        self.d, self.L, self.H, self.clamp = d, layers, hidden, float(clamp)
+        self.n_params = load().orc_flow_num_params(d, layers, hidden)
+
+    def mask(self, layer):
+        out = np.zeros(self.d, dtype=np.int32)
+        load().orc_flow_mask(self.d, self.L, self.H, layer, out.ctypes.data_as(_ip))
+        return out
+
+    def forward(self, theta, z):
+        th, z = _d(theta), _d(z)
+        x = np.zeros(self.d)
+        ld = load().orc_flow_forward(self.d, self.L, self.H, self.clamp, th.ctypes.data_as(_dp),
+                                     z.ctypes.data_as(_dp), x.ctypes.data_as(_dp))
+        return x, ld
+
+    def inverse(self, theta, x):
+        th, x = _d(theta), _d(x)
+        z = np.zeros(self.d)
+        ld = load().orc_flow_inverse(self.d, self.L, self.H, self.clamp, th.ctypes.data_as(_dp),
+                                     x.ctypes.data_as(_dp), z.ctypes.data_as(_dp))
+        return z, ld
+
+    def log_prob_grad(self, model, theta, z, jacobian=True, param_grad=False):
+        """lp_z = lp_x(T(z)) + log|det|, d lp_z / dz and (param_grad) d lp_z / dtheta."""
+        th, z = _d(theta), _d(z)
+        gz = np.zeros(self.d)
+        gth = np.zeros(self.n_params) if param_grad else None
+        x = np.zeros(self.d)
+        lpx = ctypes.c_double()
+        lp = load().orc_flow_log_prob_grad(model._h, self.L, self.H, self.clamp, th.ctypes.data_as(_dp),
+                                           z.ctypes.data_as(_dp), int(jacobian), gz.ctypes.data_as(_dp),
+                                           None if gth is None else gth.ctypes.data_as(_dp),
+                                           x.ctypes.data_as(_dp), ctypes.byref(lpx))
+        return (lp, gz, gth, x, lpx.value) if param_grad else (lp, gz)
+
+
+def adam(theta, m, v, g, t, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+    """In-place Adam step on FP64 arrays (oracle of the device Adam kernel)."""
+    for a in (theta, m, v):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    g = _d(g)
+    load().orc_adam(len(theta), theta.ctypes.data_as(_dp), m.ctypes.data_as(_dp), v.ctypes.data_as(_dp),
+                    g.ctypes.data_as(_dp), int(t), lr, b1, b2, eps)

@@ -25,8 +25,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "-I" + INC, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-I" + CSRC]
 
-CU_SOURCES = ["sampler.cu", "grad_tc.cu", "noalloc.cu"]
-CPP_SOURCES = ["abi.cpp", "summary.cpp"]
+CU_SOURCES = ["sampler.cu", "grad_tc.cu", "noalloc.cu", "flow.cu"]
+CPP_SOURCES = ["abi.cpp", "summary.cpp", "learned.cpp"]
 
 
 def _nvcc():

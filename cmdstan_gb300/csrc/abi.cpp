@@ -32,6 +32,13 @@ int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
 }
+}  // namespace
+
+int api_fail(int code, const std::string& msg) { return fail(code, msg); }
+
+int validate_args(const Model& m, const gnuts_sample_args* a, int adapt, int metric);
+
+namespace {
 
 // ---------------------------------------------------------------- var context
 struct Var {
@@ -352,6 +359,70 @@ ModelImpl* build_model(const std::string& id, const VarMap& vm) {
     for (int k = 1; k <= K; ++k) m->con_names.push_back(idx_name("beta", k));
     m->con_names.push_back("sigma_y");
     m->con_names.push_back("tau");
+  } else if (id == "varint_set") {
+    // P independent varying-intercept regressions sampled in one launch.
+    // Data: P, K, J[P], N[P], group (1-based within its posterior), X
+    // [sum N][K], y [sum N]; the rows of posterior p follow those of p - 1.
+    // fp32 (default 1) evaluates the likelihood rows in FP32.
+    d.kind = MK_VARINT;
+    int64_t P = need_int(vm, "P"), K = need_int(vm, "K");
+    if (P < 1 || K < 0 || K > 16) throw std::runtime_error("varint_set needs P >= 1 and 0 <= K <= 16");
+    const Var& Jv = need(vm, "J");
+    check_dims(Jv, "J", {P});
+    const Var& Nv = need(vm, "N");
+    check_dims(Nv, "N", {P});
+    int64_t total = 0;
+    for (int64_t p = 0; p < P; ++p) {
+      if (Jv.values[p] < 1 || Nv.values[p] < 0) throw std::runtime_error("varint_set needs J[p] >= 1 and N[p] >= 0");
+      total += (int64_t)Nv.values[p];
+    }
+    const Var& g = need(vm, "group");
+    check_dims(g, "group", {total});
+    const Var& X = need(vm, "X");
+    check_dims(X, "X", {total, K});
+    const Var& y = need(vm, "y");
+    check_dims(y, "y", {total});
+    d.fp32 = vm.count("fp32") ? (int)need_int(vm, "fp32") : 1;
+    d.alpha_last = 1;
+    h.X.resize(total * K);
+    h.yr.resize(total);
+    h.group.resize(total);
+    int64_t row = 0, goff = 0, Jmax = 0;
+    for (int64_t p = 0; p < P; ++p) {
+      const int64_t J = (int64_t)Jv.values[p], Np = (int64_t)Nv.values[p];
+      std::vector<int64_t> order(Np);
+      std::iota(order.begin(), order.end(), row);
+      for (int64_t n = row; n < row + Np; ++n) {
+        const double gv = g.values[n];
+        if (gv < 1 || gv > J || gv != std::floor(gv)) throw std::runtime_error("group must be in 1..J[p]");
+      }
+      std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return g.values[a] < g.values[b]; });
+      std::vector<int> gs(J + 1, 0);
+      for (int64_t i = 0; i < Np; ++i) {
+        const int64_t n = order[i];
+        h.group[row + i] = (int)g.values[n];
+        for (int64_t k = 0; k < K; ++k) h.X[(row + i) * K + k] = X.values[n * K + k];
+        h.yr[row + i] = y.values[n];
+        gs[(int)g.values[n]]++;
+      }
+      for (int64_t j = 1; j <= J; ++j) gs[j] += gs[j - 1];
+      h.gstart.insert(h.gstart.end(), gs.begin(), gs.end());
+      m->members.push_back({(int)Np, (int)J, (int)(J + K + 2), (long)row, (long)goff});
+      row += Np;
+      goff += J + 1;
+      Jmax = std::max(Jmax, J);
+    }
+    d.N = (int)total;
+    d.J = (int)Jmax;
+    d.K = (int)K;
+    d.D = (int)(Jmax + K + 2);
+    d.ncon = d.D;
+    d.n_members = (int)P;
+    m->name = "varint_set_model";
+    for (int k = 1; k <= K; ++k) m->con_names.push_back(idx_name("beta", k));
+    m->con_names.push_back("sigma_y");
+    m->con_names.push_back("tau");
+    for (int j = 1; j <= Jmax; ++j) m->con_names.push_back(idx_name("alpha", j));
   } else if (id == "horseshoe") {
     d.kind = MK_HORSESHOE;
     int64_t N = need_int(vm, "N");
@@ -420,7 +491,10 @@ int create(const std::string& id, const VarMap& vm, gnuts_model** out) {
 Model* M(gnuts_model* m) { return reinterpret_cast<Model*>(m); }
 const Model* M(const gnuts_model* m) { return reinterpret_cast<const Model*>(m); }
 
-int validate(const Model& m, const gnuts_sample_args* a, int adapt, int metric) {
+int validate(const Model& m, const gnuts_sample_args* a, int adapt, int metric) { return validate_args(m, a, adapt, metric); }
+}  // namespace
+
+int validate_args(const Model& m, const gnuts_sample_args* a, int adapt, int metric) {
   if (!a) return fail(GNUTS_ERR_ARGUMENT, "no arguments");
   if (a->num_chains < 1) return fail(GNUTS_ERR_ARGUMENT, "num_chains must be >= 1");
   if (a->num_warmup < 0) return fail(GNUTS_ERR_ARGUMENT, "num_warmup must be >= 0");
@@ -444,6 +518,8 @@ int validate(const Model& m, const gnuts_sample_args* a, int adapt, int metric) 
   (void)metric;
   return GNUTS_OK;
 }
+
+namespace {
 
 int service(gnuts_model* mh, const gnuts_sample_args* a, const double* inits, const double* inv_metric,
             gnuts_output* out, gnuts_progress_fn progress, void* ctx, int metric, int adapt) {
@@ -571,6 +647,7 @@ int gnuts_unconstrain(const gnuts_model* m, const double* c, double* q) {
         q[d.J + 1] = pos(c[d.J + 1], "tau");
         break;
       case MK_VARINT:
+        if (d.n_members) throw std::runtime_error("a posterior set takes unconstrained inits (one row per chain)");
         for (int i = 0; i < d.J + d.K; ++i) q[i] = c[i];
         q[d.J + d.K] = pos(c[d.J + d.K], "sigma_y");
         q[d.J + d.K + 1] = pos(c[d.J + d.K + 1], "tau");

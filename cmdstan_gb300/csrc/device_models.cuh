@@ -146,12 +146,57 @@ static __device__ __noinline__ double lpg_logistic(const DevModel& M, const doub
   return lp;
 }
 
-// ---- varint: [alpha_1..J, beta_1..K, log sigma_y, log tau]; rows sorted by group
+// ---- varint: [alpha_1..J, beta_1..K, log sigma_y, log tau]; rows sorted by group.
+// Members of a posterior set order the parameters [beta, log sigma_y, log tau,
+// alpha] (alpha_last) and may evaluate the rows in FP32 (fp32): each lane sums
+// its rows of one group in FP32 and adds the group's partial sums to FP64
+// accumulators, so the FP32 rounding never spans more than one group.
+template <class T>
+__device__ __forceinline__ void varint_rows(const DevModel& M, int r0, int r1, double a, const double* bb, double isy,
+                                            double& ss, double& gr, double* gb, int lane) {
+  const int K = M.K;
+  T b[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) b[k] = (T)(k < K ? bb[k] : 0.0);
+  const T ta = (T)a, tisy = (T)isy;
+  T s2 = 0, g1 = 0, gk[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) gk[k] = 0;
+  for (int n = r0 + lane; n < r1; n += 32) {
+    T x[16];
+    if constexpr (sizeof(T) == 4) {
+      const float* xr = M.Xf + (size_t)n * K;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.f;
+    } else {
+      const double* xr = M.X + (size_t)n * K;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.0;
+    }
+    T mu = ta;
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (k < K) mu += x[k] * b[k];
+    const T e = ((T)M.yr[n] - mu) * tisy;
+    s2 += e * e;
+    const T r = e * tisy;
+    g1 += r;
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (k < K) gk[k] += r * x[k];
+  }
+  ss += (double)s2;
+  gr = (double)g1;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) gb[k] += (double)gk[k];
+}
+
 static __device__ __noinline__ double lpg_varint(const DevModel& M, const double* q, double* g, int jac, int lane) {
   const int J = M.J, K = M.K;
-  const double* al = q;
-  const double* be = q + J;
-  double ls = q[J + K], lt = q[J + K + 1];
+  const int ib = M.alpha_last ? 0 : J, ia = M.alpha_last ? K + 2 : 0, is = M.alpha_last ? K : J + K;
+  const double* al = q + ia;
+  const double* be = q + ib;
+  double ls = q[is], lt = q[is + 1];
   double sy = exp(ls), tau = exp(lt), isy = 1.0 / sy;
   double bb[16];
 #pragma unroll
@@ -164,23 +209,11 @@ static __device__ __noinline__ double lpg_varint(const DevModel& M, const double
     double a = al[j];
     double gr = 0;
     int r0 = M.gstart[j], r1 = M.gstart[j + 1];
-    for (int n = r0 + lane; n < r1; n += 32) {
-      const double* x = M.X + (size_t)n * K;
-      double mu = a;
-#pragma unroll
-      for (int k = 0; k < 16; ++k)
-        if (k < K) mu += x[k] * bb[k];
-      double e = (M.yr[n] - mu) * isy;
-      ss += e * e;
-      double r = e * isy;
-      gr += r;
-#pragma unroll
-      for (int k = 0; k < 16; ++k)
-        if (k < K) gb[k] += r * x[k];
-    }
+    if (M.fp32) varint_rows<float>(M, r0, r1, a, bb, isy, ss, gr, gb, lane);
+    else varint_rows<double>(M, r0, r1, a, bb, isy, ss, gr, gb, lane);
     gr = wsum(gr);
     double z = a / tau;
-    if (lane == 0) g[j] = gr - z / tau;
+    if (lane == 0) g[ia + j] = gr - z / tau;
     lpa += -lt - 0.5 * z * z;
     glt += -1.0 + z * z;
   }
@@ -190,7 +223,7 @@ static __device__ __noinline__ double lpg_varint(const DevModel& M, const double
   for (int k = 0; k < 16; ++k) {
     if (k < K) {
       double t = wsum(gb[k]);
-      if (lane == 0) g[J + k] = t - bb[k];
+      if (lane == 0) g[ib + k] = t - bb[k];
       pb += -0.5 * bb[k] * bb[k];
     }
   }
@@ -204,8 +237,8 @@ static __device__ __noinline__ double lpg_varint(const DevModel& M, const double
     glt += 1.0;
   }
   if (lane == 0) {
-    g[J + K] = gls;
-    g[J + K + 1] = glt;
+    g[is] = gls;
+    g[is + 1] = glt;
   }
   return lp;
 }
@@ -302,6 +335,11 @@ __device__ __forceinline__ double warp_log_prob_grad(const DevModel& M, const do
   return __longlong_as_double(0x7ff8000000000000ll);
 }
 
+// the model a chain (or point) c of C evaluates: itself, or its posterior-set member
+__device__ __forceinline__ const DevModel& chain_model(const DevModel& M, int c, int C) {
+  return M.members ? M.members[c / (C / M.n_members)] : M;
+}
+
 // write_array: unconstrained q -> constrained output columns (warp-parallel)
 __device__ __forceinline__ void warp_write_array(const DevModel& M, const double* q, double* out,
                                                  int lane) {
@@ -317,9 +355,11 @@ __device__ __forceinline__ void warp_write_array(const DevModel& M, const double
     case MK_HIER:
       for (int i = lane; i < M.D; i += 32) out[i] = (i == M.J + 1) ? exp(q[i]) : q[i];
       return;
-    case MK_VARINT:
-      for (int i = lane; i < M.D; i += 32) out[i] = (i >= M.J + M.K) ? exp(q[i]) : q[i];
+    case MK_VARINT: {
+      const int is = M.alpha_last ? M.K : M.J + M.K;
+      for (int i = lane; i < M.D; i += 32) out[i] = (i == is || i == is + 1) ? exp(q[i]) : q[i];
       return;
+    }
     case MK_HORSESHOE: {
       const int D = M.K;
       double tau = exp(q[D + 1]), caux = exp(q[2 * D + 2]);

@@ -40,6 +40,13 @@ struct DevModel {
   // y packed 32 rows per word
   const uint16_t* Xtc;
   const uint32_t* ybits;
+  // varint: parameter order [beta, log sigma_y, log tau, alpha] (posterior
+  // sets, so that the shared parameters sit in the same columns for every
+  // posterior) and FP32 likelihood rows (FP64 sums across groups)
+  int alpha_last, fp32;
+  // posterior set: chain (or point) c of C uses members[c / (C / n_members)]
+  const DevModel* members;
+  int n_members;
 };
 constexpr int XTC_LD = 104;  // row stride in elements (208 B, a multiple of 16 B)
 
@@ -53,12 +60,34 @@ struct Model {
   std::vector<int> host_yi;
   std::vector<void*> device_allocs;
   int device = -1;
+  // posterior set: members with row / group offsets into the shared arrays
+  struct Member { int N, J, D; long row_off, g_off; };
+  std::vector<Member> members;
   ~Model();
+};
+
+// Affine-coupling flow (flow.cu): host-side layout plus device buffers.
+struct Flow {
+  int d = 0, L = 0, H = 0;
+  float clamp = 4.0f;
+  std::vector<int> nb, na, idx, idx_off;  // idx: per layer b list then a list
+  std::vector<long> th_off, w_off;        // th_off has L + 1 entries (th_off[L] = mu)
+  long th_rho = 0, n_params = 0, n_w16 = 0;
+  int stage_max = 0;
+  int device = -1;
+  float *theta = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
+  uint16_t* w16 = nullptr;
+  int* didx = nullptr;
+  int* nvalid = nullptr;  // [2] valid-point counters of the training steps
+  ~Flow();
 };
 
 struct RunConfig {
   int metric;   // 0 diag, 1 dense, 2 unit
   int adapt;
+  const Flow* flow = nullptr;      // sample z with x = T(z) (learned preconditioner)
+  const double* stepsizes = nullptr;  // per-chain initial step size (NULL: the argument's)
+  double* q_last = nullptr;        // [C][D] final sampler-space position of every chain
 };
 
 // sampler.cu
@@ -73,6 +102,22 @@ int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, int precis
                       std::string& err);
 int run_write_array(Model& m, int n, const double* q, double* out, std::string& err);
 int upload(Model& m, std::string& err);
+// abi.cpp: record the calling thread's last error (returns code); argument checks of the services
+int api_fail(int code, const std::string& msg);
+int validate_args(const Model& m, const gnuts_sample_args* a, int adapt, int metric);
+
+// flow.cu
+int flow_create(int d, int L, int H, double clamp, Flow** out, std::string& err);
+int flow_set_params(Flow& f, const double* theta, std::string& err);
+int flow_get_params(const Flow& f, double* theta, std::string& err);
+int flow_forward(Flow& f, int n, const double* z, double* x, double* logdet, std::string& err);
+int flow_inverse(Flow& f, int n, const double* x, double* z, double* logdet, std::string& err);
+int flow_log_prob_grad(Model& m, Flow& f, int n, const double* z, int jacobian, double* lp, double* grad_z,
+                       double* grad_theta, std::string& err);
+int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, double b2, double eps,
+                   std::string& err);
+int flow_train(Model& m, Flow& f, int steps, int batch, double lr, double base_scale, unsigned seed,
+               double* loss_trace, std::string& err);
 // noalloc.cu: the allocation-free batched gradient (device pointers)
 int noalloc_log_prob_grad(const Model& m, int n, const double* q, int jac, double* lp, double* g, std::string& err);
 

@@ -84,6 +84,8 @@ struct Bufs {
   double* out_minv;    // [C][D] or [C][D*D]
   const double* init_q;  // [C][D] (has_init)
   const double* p0;      // [C][D] (replay)
+  const double* init_eps;  // [C] per-chain initial step size (null: P.stepsize)
+  double* zdraws;        // [C][n_saved][D]: sampler-space draws (flow runs; write_array happens later)
   Scal* sc;
   int* done_count;
 };
@@ -118,7 +120,7 @@ struct Chain {
   double* cache_base = nullptr;
 
   __device__ Chain(const Params& p, const Bufs& b, const DevModel& m, Scal& sc, int ci, int ln)
-      : P(p), B(b), M(m), s(sc), c(ci), lane(ln), D(p.D) {
+      : P(p), B(b), M(m), s(sc), c(ci), lane(ln), D(m.D) {
     rsc = b.recs + (size_t)ci * p.R * 3;
     chain_id = p.id_base + (uint32_t)ci;
     size_t o = (size_t)ci * p.ld;
@@ -332,7 +334,7 @@ struct Chain {
   // draws a candidate into W.q (stream 1), gradient then requested
   __device__ void init_candidate() {
     if (P.has_init) {
-      for (int d = lane; d < D; d += 32) Wq[d] = B.init_q[(size_t)c * D + d];
+      for (int d = lane; d < D; d += 32) Wq[d] = B.init_q[(size_t)c * P.D + d];
     } else {
       const uint64_t n0 = s.irng_n;
       for (int d = lane; d < D; d += 32)
@@ -407,7 +409,7 @@ struct Chain {
       if (P.adapt) s.nom_eps = exp(s.da_xbar);  // complete_adaptation
       s.t_warm = globaltimer();
       if (lane == 0) B.out_eps[c] = s.nom_eps;
-      const size_t msz = P.metric == 1 ? (size_t)D * D : (size_t)D;
+      const size_t msz = P.metric == 1 ? (size_t)D * D : (size_t)P.D;
       if (P.metric == 1) {
         for (int i = 0; i < D; ++i)
           for (int j = lane; j < D; j += 32) B.out_minv[(size_t)c * msz + (size_t)i * D + j] = minv[(size_t)i * P.ld + j];
@@ -419,7 +421,7 @@ struct Chain {
     if (P.jitter > 0 && !P.replay) s.eps *= 1.0 + P.jitter * (2.0 * uniform() - 1.0);
     load_W_from(Sq, nullptr, Sg, s.S_lp);
     if (P.replay) {
-      for (int d = lane; d < D; d += 32) Wp[d] = B.p0[(size_t)c * D + d];
+      for (int d = lane; d < D; d += 32) Wp[d] = B.p0[(size_t)c * P.D + d];
       __syncwarp();
     } else {
       sample_p(Wp);
@@ -659,7 +661,14 @@ struct Chain {
       row[0] = s.S_lp; row[1] = accept; row[2] = s.eps; row[3] = s.depth;
       row[4] = s.n_leapfrog; row[5] = s.divergent; row[6] = s.S_h;
     }
-    warp_write_array(M, Sq, row + 7, lane);
+    if (B.zdraws) {
+      double* zr = B.zdraws + ((size_t)c * P.n_saved + s.row) * P.D;
+      for (int d = lane; d < D; d += 32) zr[d] = Sq[d];
+    } else {
+      warp_write_array(M, Sq, row + 7, lane);
+      // columns past this chain's model (a smaller member of a posterior set)
+      for (int i = M.ncon + lane; i < P.ncon; i += 32) row[7 + i] = __longlong_as_double(0x7ff8000000000000ll);
+    }
     ++s.row;
   }
 

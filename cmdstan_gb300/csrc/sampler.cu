@@ -44,14 +44,15 @@ __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, R
   if (warp >= P.C) return;
   Scal s;
   memset(&s, 0, sizeof(Scal));
-  Chain ch(P, B, M, s, warp, lane);
+  Chain ch(P, B, chain_model(M, warp, P.C), s, warp, lane);
   if (RB.chain_ids) ch.chain_id = RB.chain_ids[warp];
   s.t_start = globaltimer();
-  s.nom_eps = P.stepsize;
-  s.eps = P.stepsize;
+  const double eps0 = B.init_eps ? B.init_eps[warp] : P.stepsize;
+  s.nom_eps = eps0;
+  s.eps = eps0;
   s.rng_n = RB.rng_start ? RB.rng_start[warp] : 0ull;
   s.irng_n = 0;
-  s.da_mu = log(10.0 * P.stepsize);
+  s.da_mu = log(10.0 * eps0);
   // windowed_adaptation::set_window_params
   {
     unsigned nw = (unsigned)P.num_warmup;
@@ -107,12 +108,13 @@ __global__ void __launch_bounds__(128) k_fused(Params P, Bufs B, DevModel M, Rep
   if (warp >= P.C) return;
   Scal s = B.sc[warp];
   if (s.phase >= PH_DONE) return;
-  Chain ch(P, B, M, s, warp, lane);
+  const DevModel& Mc = chain_model(M, warp, P.C);
+  Chain ch(P, B, Mc, s, warp, lane);
   if (RB.chain_ids) ch.chain_id = RB.chain_ids[warp];
   extern __shared__ double gn_cache[];
   if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
   for (int b = 0; b < P.grad_budget; ++b) {
-    double lp = warp_log_prob_grad(M, ch.Wq, ch.Wg, 1, lane);
+    double lp = warp_log_prob_grad(Mc, ch.Wq, ch.Wg, 1, lane);
     __syncwarp();
     s.W_lp = lp;
     if (!ch.advance()) break;
@@ -146,7 +148,8 @@ __global__ void k_log_prob_grad(DevModel M, int n, const double* q, int jac, dou
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
-  double v = warp_log_prob_grad(M, q + (size_t)warp * M.D, g + (size_t)warp * M.D, jac, lane);
+  const DevModel& Mc = chain_model(M, warp, n);
+  double v = warp_log_prob_grad(Mc, q + (size_t)warp * M.D, g + (size_t)warp * M.D, jac, lane);
   if (lane == 0) lp[warp] = v;
 }
 
@@ -182,7 +185,10 @@ __global__ void k_write_array(DevModel M, int n, const double* q, double* out) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
-  warp_write_array(M, q + (size_t)warp * M.D, out + (size_t)warp * M.ncon, lane);
+  const DevModel& Mc = chain_model(M, warp, n);
+  double* o = out + (size_t)warp * M.ncon;
+  warp_write_array(Mc, q + (size_t)warp * M.D, o, lane);
+  for (int i = Mc.ncon + lane; i < M.ncon; i += 32) o[i] = __longlong_as_double(0x7ff8000000000000ll);
 }
 
 // ---------------------------------------------------------------- host side
@@ -306,9 +312,32 @@ int upload(Model& m, std::string& err) {
     if (e != cudaSuccess) { err = std::string("deriving X copies: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
   }
   if (h.group && (rc = put(h.group, sizeof(int) * h.N, (void**)&d.group))) return rc;
-  if (h.gstart && (rc = put(h.gstart, sizeof(int) * (h.J + 1), (void**)&d.gstart))) return rc;
+  size_t n_gstart = (size_t)h.J + 1;
+  if (!m.members.empty()) n_gstart = (size_t)(m.members.back().g_off + m.members.back().J + 1);
+  if (h.gstart && (rc = put(h.gstart, sizeof(int) * n_gstart, (void**)&d.gstart))) return rc;
   if (h.sigma && (rc = put(h.sigma, sizeof(double) * h.J, (void**)&d.sigma))) return rc;
   if (h.scales && (rc = put(h.scales, sizeof(double) * h.K, (void**)&d.scales))) return rc;
+  if (!m.members.empty()) {
+    // one DevModel per posterior, pointing into the shared device arrays
+    std::vector<DevModel> mem(m.members.size());
+    for (size_t i = 0; i < mem.size(); ++i) {
+      const Model::Member& s = m.members[i];
+      DevModel e = d;
+      e.N = s.N;
+      e.J = s.J;
+      e.D = s.D;
+      e.ncon = s.D;
+      e.X = d.X + (size_t)s.row_off * d.K;
+      e.Xf = d.Xf + (size_t)s.row_off * d.K;
+      e.Xb = d.Xb + (size_t)s.row_off * d.K;
+      e.yr = d.yr + s.row_off;
+      e.gstart = d.gstart + s.g_off;
+      e.members = nullptr;
+      e.n_members = 0;
+      mem[i] = e;
+    }
+    if ((rc = put(mem.data(), sizeof(DevModel) * mem.size(), (void**)&d.members))) return rc;
+  }
   m.dev = d;
   cudaGetDevice(&m.device);
   return GNUTS_OK;
@@ -541,6 +570,11 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                          const double* inv_metric, const double* p0, const unsigned* chain_ids,
                          uint64_t* counters, double* replay_q_out, gnuts_output* out,
                          gnuts_progress_fn progress, void* ctx, std::string& err);
+// flow.cu
+int run_flow_rounds(Model& m, const Flow& f, const Params& P, const Bufs& B, double per_chain_max, double* stats,
+                    std::string& err);
+int flow_finalize_draws(Model& m, const Flow& f, int rows, const double* zdraws, double* draws, int ncol,
+                        std::string& err);
 
 int run_nuts(Model& m, const gnuts_sample_args& a, const RunConfig& rc, const double* inits,
              const double* inv_metric, gnuts_output* out, gnuts_progress_fn progress, void* ctx,
@@ -556,6 +590,11 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   if (st) return st;
   if ((st = check_warp_limits(m, err))) return st;
   const int C = a.num_chains, D = m.dev.D;
+  if (m.dev.n_members && (C % m.dev.n_members != 0 || rc.flow)) {
+    err = "a posterior set needs num_chains to be a multiple of its " + std::to_string(m.dev.n_members) +
+          " posteriors (and no flow)";
+    return GNUTS_ERR_ARGUMENT;
+  }
   Params P{};
   P.C = C;
   P.D = D;
@@ -633,6 +672,19 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     GN_CUDA(cudaMemcpy(d, p0, sizeof(double) * C * D, cudaMemcpyHostToDevice));
     B.p0 = d;
   }
+  if (rc.stepsizes) {
+    double* d;
+    GN_CUDA(ar.alloc(&d, (size_t)C));
+    GN_CUDA(cudaMemcpy(d, rc.stepsizes, sizeof(double) * C, cudaMemcpyHostToDevice));
+    B.init_eps = d;
+  }
+  if (rc.flow) {
+    if (rc.flow->d != D || p0) {
+      err = "flow dimension does not match the model's";
+      return GNUTS_ERR_ARGUMENT;
+    }
+    GN_CUDA(ar.alloc(&B.zdraws, (size_t)C * P.n_saved * D));
+  }
   ReplayBufs RB{nullptr, nullptr};
   if (chain_ids) {
     unsigned* d;
@@ -659,7 +711,20 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                                8.0 * 1200.0 + 200.0;
   int done = 0;
   RunStats stats;
-  if (use_rounds(m) && !p0) {
+  if (rc.flow) {
+    double fs[3] = {0, 0, 0};
+    st = run_flow_rounds(m, *rc.flow, P, B, per_chain_max, fs, err);
+    if (st) return st;
+    stats.rounds = fs[0];
+    stats.device_ms = fs[1];
+    stats.launches = fs[2];
+    GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
+    if (done >= C) {
+      st = flow_finalize_draws(m, *rc.flow, C * P.n_saved, B.zdraws, B.draws, P.ncol, err);
+      if (st) return st;
+      stats.launches += 1;
+    }
+  } else if (use_rounds(m) && !p0) {
     st = run_rounds(m, P, B, a.precision, per_chain_max, a.refresh, progress, ctx, stats, err);
     if (st) return st;
     GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
@@ -740,6 +805,9 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   if (replay_q_out)
     GN_CUDA(cudaMemcpy2D(replay_q_out, sizeof(double) * D, B.Sq, sizeof(double) * P.ld, sizeof(double) * D, C,
                          cudaMemcpyDeviceToHost));
+  if (rc.q_last)
+    GN_CUDA(cudaMemcpy2D(rc.q_last, sizeof(double) * D, B.Sq, sizeof(double) * P.ld, sizeof(double) * D, C,
+                         cudaMemcpyDeviceToHost));
   return GNUTS_OK;
 }
 
@@ -777,11 +845,21 @@ int run_transition(Model& m, int metric, const double* inv_metric, int n, const 
   return GNUTS_OK;
 }
 
+static int check_points(const Model& m, int n, std::string& err) {
+  if (m.dev.n_members && n % m.dev.n_members != 0) {
+    err = "a posterior set evaluates a multiple of its " + std::to_string(m.dev.n_members) +
+          " posteriors' points (point i belongs to posterior i / (n / P))";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  return GNUTS_OK;
+}
+
 int run_log_prob_grad(Model& m, int n, const double* q, int jacobian, int precision, double* lp, double* grad,
                       std::string& err) {
   int st = upload(m, err);
   if (st) return st;
   if (n <= 0) return GNUTS_OK;
+  if ((st = check_points(m, n, err))) return st;
   const int D = m.dev.D;
   Arena ar;
   double *dq, *dg, *dl;
@@ -807,6 +885,7 @@ int run_write_array(Model& m, int n, const double* q, double* out, std::string& 
   int st = upload(m, err);
   if (st) return st;
   if (n <= 0) return GNUTS_OK;
+  if ((st = check_points(m, n, err))) return st;
   const int D = m.dev.D, K = m.dev.ncon;
   Arena ar;
   double *dq, *dout;

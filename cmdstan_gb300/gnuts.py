@@ -32,6 +32,10 @@ EXPORTS = [
     "gnuts_hmc_nuts_dense_e_adapt", "gnuts_hmc_nuts_unit_e_adapt", "gnuts_hmc_nuts_diag_e",
     "gnuts_hmc_nuts_dense_e", "gnuts_hmc_nuts_unit_e", "gnuts_transition", "gnuts_last_error",
     "gnuts_version", "gnuts_summary", "gnuts_summary_columns", "gnuts_log_prob_grad_noalloc",
+    "gnuts_flow_create", "gnuts_flow_destroy", "gnuts_flow_num_params", "gnuts_flow_set_params",
+    "gnuts_flow_get_params", "gnuts_flow_init_affine", "gnuts_flow_forward", "gnuts_flow_inverse",
+    "gnuts_flow_log_prob_grad", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
+    "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt",
 ]
 SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
 
@@ -100,6 +104,26 @@ class Output(ctypes.Structure):
                 ("timing", ctypes.c_void_p)]
 
 
+class LearnedArgs(ctypes.Structure):
+    _fields_ = [("layers", ctypes.c_int), ("hidden", ctypes.c_int), ("clamp", ctypes.c_double),
+                ("train_steps", ctypes.c_int), ("batch", ctypes.c_int), ("learning_rate", ctypes.c_double),
+                ("base_scale", ctypes.c_double), ("flow_warmup", ctypes.c_int), ("pilot_samples", ctypes.c_int),
+                ("moment_tolerance", ctypes.c_double)]
+
+
+class LearnedReport(ctypes.Structure):
+    _fields_ = [("used_flow", ctypes.c_int), ("plain_ess_per_grad", ctypes.c_double),
+                ("flow_ess_per_grad", ctypes.c_double), ("plain_divergence_rate", ctypes.c_double),
+                ("flow_divergence_rate", ctypes.c_double), ("max_moment_z", ctypes.c_double),
+                ("loss_first", ctypes.c_double), ("loss_last", ctypes.c_double),
+                ("plain_seconds", ctypes.c_double), ("train_seconds", ctypes.c_double),
+                ("flow_seconds", ctypes.c_double), ("final_seconds", ctypes.c_double),
+                ("plain_grads", ctypes.c_int64), ("flow_grads", ctypes.c_int64), ("final_grads", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "launches", "reduce_kernel_us"]
 
 
@@ -146,6 +170,26 @@ def load():
     i64 = ctypes.c_int64
     lib.gnuts_summary.argtypes = [dp, ip, ip, i64, i64, dp, ip, dp]
     lib.gnuts_summary_columns.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, ip, dp]
+    lib.gnuts_flow_create.argtypes = [ip, ip, ip, ctypes.c_double, ctypes.POINTER(vp)]
+    lib.gnuts_flow_destroy.argtypes = [vp]
+    lib.gnuts_flow_destroy.restype = None
+    lib.gnuts_flow_num_params.argtypes = [vp]
+    lib.gnuts_flow_num_params.restype = ctypes.c_long
+    lib.gnuts_flow_set_params.argtypes = [vp, dp]
+    lib.gnuts_flow_get_params.argtypes = [vp, dp]
+    lib.gnuts_flow_init_affine.argtypes = [vp, dp, dp, ctypes.c_uint, ctypes.c_double]
+    lib.gnuts_flow_forward.argtypes = [vp, ip, dp, dp, dp]
+    lib.gnuts_flow_inverse.argtypes = [vp, ip, dp, dp, dp]
+    lib.gnuts_flow_log_prob_grad.argtypes = [vp, vp, ip, dp, ip, dp, dp, dp]
+    lib.gnuts_flow_adam_step.argtypes = [vp, dp, ip] + [ctypes.c_double] * 4
+    lib.gnuts_flow_train.argtypes = [vp, vp, ip, ip, ctypes.c_double, ctypes.c_double, ctypes.c_uint, dp]
+    lib.gnuts_hmc_nuts_flow_diag_e_adapt.argtypes = [vp, vp, ctypes.POINTER(SampleArgs), dp, dp,
+                                                     ctypes.POINTER(Output), PROGRESS_FN, vp]
+    lib.gnuts_learned_args_default.argtypes = [ctypes.POINTER(LearnedArgs)]
+    lib.gnuts_learned_args_default.restype = None
+    lib.gnuts_hmc_nuts_learned_diag_e_adapt.argtypes = [vp, ctypes.POINTER(SampleArgs), ctypes.POINTER(LearnedArgs),
+                                                        dp, ctypes.POINTER(Output), ctypes.POINTER(LearnedReport),
+                                                        PROGRESS_FN, vp]
     _lib = lib
     return lib
 
@@ -264,6 +308,24 @@ class Model:
         return out
 
     # -- services
+    def _outputs(self, a, mk, n_saved):
+        C, D = a.num_chains, self.dim
+        ncol = 7 + self.num_constrained
+        msz = D * D if mk == 1 else D
+        bufs = dict(draws=np.zeros((C, n_saved, ncol)), eps=np.zeros(C), minv=np.zeros((C, msz)), tw=np.zeros(C),
+                    ts=np.zeros(C), ng=np.zeros(C, dtype=np.int64), stt=np.zeros(C, dtype=np.int32),
+                    nlf=np.zeros(C, dtype=np.int64), tim=np.zeros(8))
+        b = bufs
+        out = Output(b["draws"].ctypes.data, b["eps"].ctypes.data, b["minv"].ctypes.data, b["tw"].ctypes.data,
+                     b["ts"].ctypes.data, b["ng"].ctypes.data, b["stt"].ctypes.data, b["nlf"].ctypes.data,
+                     b["tim"].ctypes.data)
+        return out, bufs
+
+    def _fit(self, b, mk):
+        minv = b["minv"].reshape(len(b["eps"]), self.dim, self.dim) if mk == 1 else b["minv"]
+        return Fit(SAMPLER_COLUMNS + self.param_names, b["draws"], b["eps"], minv, b["tw"], b["ts"], b["ng"],
+                   b["stt"], b["nlf"], b["tim"][:len(TIMING_FIELDS)])
+
     def sample(self, metric="diag_e", adapt=True, inits=None, inv_metric=None, progress=None, **kw):
         """Run hmc_nuts_<metric>[_adapt]; keyword arguments are gnuts_sample_args fields."""
         a = default_args(**kw)
@@ -271,18 +333,8 @@ class Model:
         mk = METRICS[metric]
         th = max(1, a.thin)  # the library rejects thin < 1 itself
         n_saved = max(0, ((a.num_warmup + th - 1) // th if a.save_warmup else 0) + (a.num_samples + th - 1) // th)
-        ncol = 7 + self.num_constrained
-        draws = np.zeros((C, n_saved, ncol))
-        eps = np.zeros(C)
         msz = D * D if mk == 1 else D
-        minv = np.zeros((C, msz))
-        tw, ts = np.zeros(C), np.zeros(C)
-        ng = np.zeros(C, dtype=np.int64)
-        stt = np.zeros(C, dtype=np.int32)
-        nlf = np.zeros(C, dtype=np.int64)
-        tim = np.zeros(8)
-        out = Output(draws.ctypes.data, eps.ctypes.data, minv.ctypes.data, tw.ctypes.data, ts.ctypes.data,
-                     ng.ctypes.data, stt.ctypes.data, nlf.ctypes.data, tim.ctypes.data)
+        out, b = self._outputs(a, mk, n_saved)
         if inits is not None:
             inits = np.ascontiguousarray(np.broadcast_to(np.asarray(inits, dtype=np.float64), (C, D)))
         if inv_metric is not None:
@@ -299,10 +351,37 @@ class Model:
         else:
             rc = fn(self._h, ctypes.byref(a), _dp(inits), _dp(im), ctypes.byref(out), cb, None)
         _check(rc)
-        if mk == 1:
-            minv = minv.reshape(C, D, D)
-        return Fit(SAMPLER_COLUMNS + self.param_names, draws, eps, minv, tw, ts, ng, stt, nlf,
-                   tim[:len(TIMING_FIELDS)])
+        return self._fit(b, mk)
+
+    def sample_flow(self, flow, inits_z=None, inv_metric=None, **kw):
+        """hmc_nuts_diag_e_adapt on z with x = flow(z); draws are reported in x."""
+        a = default_args(**kw)
+        C, D = a.num_chains, self.dim
+        th = max(1, a.thin)
+        n_saved = max(0, ((a.num_warmup + th - 1) // th if a.save_warmup else 0) + (a.num_samples + th - 1) // th)
+        out, b = self._outputs(a, 0, n_saved)
+        z0 = None if inits_z is None else np.ascontiguousarray(np.broadcast_to(inits_z, (C, D)), dtype=np.float64)
+        im = None if inv_metric is None else np.ascontiguousarray(np.broadcast_to(inv_metric, (C, D)),
+                                                                   dtype=np.float64)
+        _check(self._lib.gnuts_hmc_nuts_flow_diag_e_adapt(self._h, flow._h, ctypes.byref(a), _dp(z0), _dp(im),
+                                                          ctypes.byref(out), PROGRESS_FN(), None))
+        return self._fit(b, 0)
+
+    def sample_learned(self, inits=None, learned=None, **kw):
+        """Learned-preconditioner NUTS (plain diag_e as fallback and judge).
+        Returns (Fit of the final draws, report dict)."""
+        a = default_args(**kw)
+        la = learned_args(**(learned or {}))
+        C, D = a.num_chains, self.dim
+        th = max(1, a.thin)
+        n_saved = max(0, (a.num_samples + th - 1) // th)
+        out, b = self._outputs(a, 0, n_saved)
+        ini = None if inits is None else np.ascontiguousarray(np.broadcast_to(inits, (C, D)), dtype=np.float64)
+        rep = LearnedReport()
+        _check(self._lib.gnuts_hmc_nuts_learned_diag_e_adapt(self._h, ctypes.byref(a), ctypes.byref(la), _dp(ini),
+                                                             ctypes.byref(out), ctypes.byref(rep), PROGRESS_FN(),
+                                                             None))
+        return self._fit(b, 0), rep.as_dict()
 
     def transition(self, q0, p0, stepsize, inv_metric=None, metric="diag_e", max_depth=10, seed=0,
                    chain_ids=None, counters=None):
@@ -320,3 +399,76 @@ class Model:
                                           seed, ids.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
                                           ctr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _dp(qo), _dp(st)))
         return qo, st, ctr
+
+
+def learned_args(**kw):
+    la = LearnedArgs()
+    load().gnuts_learned_args_default(ctypes.byref(la))
+    for k, v in kw.items():
+        if not hasattr(la, k):
+            raise TypeError("unknown learned-sampler argument %r" % k)
+        setattr(la, k, v)
+    return la
+
+
+class Flow:
+    """Affine-coupling flow on the GPU (gnuts_flow handle)."""
+
+    def __init__(self, dim, layers=8, hidden=128, clamp=4.0):
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.gnuts_flow_create(dim, layers, hidden, float(clamp), ctypes.byref(h)))
+        self._h, self._lib = h, lib
+        self.dim, self.layers, self.hidden, self.clamp = dim, layers, hidden, float(clamp)
+        self.n_params = lib.gnuts_flow_num_params(h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.gnuts_flow_destroy(h)
+            self._h = None
+
+    def set_params(self, theta):
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        assert t.shape == (self.n_params,)
+        _check(self._lib.gnuts_flow_set_params(self._h, _dp(t)))
+
+    def get_params(self):
+        t = np.zeros(self.n_params)
+        _check(self._lib.gnuts_flow_get_params(self._h, _dp(t)))
+        return t
+
+    def init_affine(self, mean, scale, seed=0, w1_scale=0.5):
+        m = np.ascontiguousarray(np.broadcast_to(mean, (self.dim,)), dtype=np.float64)
+        s = np.ascontiguousarray(np.broadcast_to(scale, (self.dim,)), dtype=np.float64)
+        _check(self._lib.gnuts_flow_init_affine(self._h, _dp(m), _dp(s), seed, float(w1_scale)))
+
+    def forward(self, z):
+        z = np.ascontiguousarray(np.atleast_2d(z), dtype=np.float64)
+        x, ld = np.zeros_like(z), np.zeros(z.shape[0])
+        _check(self._lib.gnuts_flow_forward(self._h, z.shape[0], _dp(z), _dp(x), _dp(ld)))
+        return x, ld
+
+    def inverse(self, x):
+        x = np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64)
+        z, ld = np.zeros_like(x), np.zeros(x.shape[0])
+        _check(self._lib.gnuts_flow_inverse(self._h, x.shape[0], _dp(x), _dp(z), _dp(ld)))
+        return z, ld
+
+    def log_prob_grad(self, model, z, jacobian=True, param_grad=False):
+        z = np.ascontiguousarray(np.atleast_2d(z), dtype=np.float64)
+        n = z.shape[0]
+        lp, gz = np.zeros(n), np.zeros_like(z)
+        gth = np.zeros(self.n_params) if param_grad else None
+        _check(self._lib.gnuts_flow_log_prob_grad(model._h, self._h, n, _dp(z), int(bool(jacobian)), _dp(lp),
+                                                  _dp(gz), _dp(gth)))
+        return (lp, gz, gth) if param_grad else (lp, gz)
+
+    def adam_step(self, grad, t, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        g = np.ascontiguousarray(grad, dtype=np.float64)
+        _check(self._lib.gnuts_flow_adam_step(self._h, _dp(g), int(t), lr, beta1, beta2, eps))
+
+    def train(self, model, steps, batch=256, lr=2e-3, seed=0, base_scale=1.0):
+        trace = np.zeros(max(1, steps))
+        _check(self._lib.gnuts_flow_train(model._h, self._h, steps, batch, lr, float(base_scale), seed, _dp(trace)))
+        return trace[:steps]

@@ -90,3 +90,22 @@ def horseshoe(seed=0, N=200_000, D=1000, n_nonzero=20):
     eta = X @ beta
     y = (g.random(N) < 1.0 / (1.0 + np.exp(-eta))).astype(np.int32)
     return {"N": N, "D": D, "X": X, "y": y, "scale_global": 0.01, "slab_scale": 2.0, "slab_df": 4.0}
+
+
+def varint_set(seed=0, P=512, K=10, Jmin=8, Jmax=256):
+    """P independent varying-intercept regressions (each drawn by varint() with
+    its own seed) concatenated for one batched launch: rows of posterior p
+    follow those of posterior p - 1."""
+    parts = [varint(seed=1_000_003 * (seed + 1) + p, K=K, Jmin=Jmin, Jmax=Jmax) for p in range(P)]
+    return {"P": P, "K": K, "J": np.array([q["J"] for q in parts], dtype=np.int32),
+            "N": np.array([q["N"] for q in parts], dtype=np.int32),
+            "group": np.concatenate([q["group"] for q in parts]).astype(np.int32),
+            "X": np.concatenate([q["X"] for q in parts]), "y": np.concatenate([q["y"] for q in parts])}
+
+
+def varint_set_member(data, p):
+    """Posterior p of a varint_set data dict as a stand-alone varint data dict."""
+    off = int(np.sum(data["N"][:p]))
+    n = int(data["N"][p])
+    return {"N": n, "J": int(data["J"][p]), "K": int(data["K"]), "group": data["group"][off:off + n],
+            "X": data["X"][off:off + n], "y": data["y"][off:off + n]}

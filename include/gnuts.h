@@ -205,6 +205,91 @@ int gnuts_summary_columns(const double* draws, int n_chains, int n_iter, int n_c
 int gnuts_log_prob_grad_noalloc(const gnuts_model* m, int n, const double* q_device, int jacobian,
                                 double* lp_device, double* grad_device);
 
+
+/* ---- learned preconditioner: affine-coupling flow ----
+ * No counterpart in the reference: CmdStan's NUTS samples the model's own
+ * unconstrained space.  A flow T maps z to x (RealNVP coupling layers with a
+ * tanh hidden layer and a soft-clamped log-scale, then x = mu + exp(rho) .* u);
+ * NUTS then samples z with target lp_x(T(z)) + log|det dT/dz|.  Parameters are
+ * one vector theta: per layer W1 [n_b][H], b1 [H], W2 [H][2 n_a], b2 [2 n_a];
+ * then mu [d], rho [d].  Layer l keeps the indices i whose bit (l mod B) equals
+ * (l div B) mod 2 (B = ceil(log2 d)) and transforms the others. */
+typedef struct gnuts_flow gnuts_flow;
+/* dim 2..128, layers 1..16, hidden 32 / 64 / 128, clamp > 0 (log-scale bound) */
+int gnuts_flow_create(int dim, int layers, int hidden, double clamp, gnuts_flow** out);
+void gnuts_flow_destroy(gnuts_flow* f);
+long gnuts_flow_num_params(const gnuts_flow* f);
+int gnuts_flow_set_params(gnuts_flow* f, const double* theta);
+int gnuts_flow_get_params(const gnuts_flow* f, double* theta);
+/* identity coupling layers (W2 = b2 = 0, b1 = 0, W1 ~ N(0, w1_scale^2 / n_b)
+ * from seed) around the affine map x = mean + scale .* z */
+int gnuts_flow_init_affine(gnuts_flow* f, const double* mean, const double* scale, unsigned int seed,
+                           double w1_scale);
+/* x = T(z) and log|det| for n points (n x dim) */
+int gnuts_flow_forward(gnuts_flow* f, int n, const double* z, double* x, double* logdet);
+/* z = T^-1(x); logdet receives log|det dT/dz| at that z (may be NULL) */
+int gnuts_flow_inverse(gnuts_flow* f, int n, const double* x, double* z, double* logdet);
+/* pulled-back log density lp = lp_x(T(z)) + log|det| (model log_prob_grad
+ * contract, command_helper.hpp:589-593, evaluated at x), its gradient in z
+ * (n x dim) and, when grad_theta is not NULL, the sum over the n points of its
+ * gradient in theta (num_params) */
+int gnuts_flow_log_prob_grad(gnuts_model* m, gnuts_flow* f, int n, const double* z, int jacobian, double* lp,
+                             double* grad_z, double* grad_theta);
+/* one Adam step (bias-corrected, step t >= 1) with the given gradient */
+int gnuts_flow_adam_step(gnuts_flow* f, const double* grad, int t, double lr, double beta1, double beta2,
+                         double eps);
+/* reverse-KL training: each step draws `batch` base points
+ * z ~ N(0, base_scale^2 I) (Philox stream 2 of (seed, point)) and minimises
+ * the mean of -(lp_x(T(z)) + log|det|) with Adam (0.9, 0.999, 1e-8; learning
+ * rate decaying linearly from lr to lr / 10).  The minimiser pulls the
+ * posterior back to N(0, base_scale^2 I): base_scale 1 is the reverse KL;
+ * larger values weight the tails more.  loss_trace (steps, may be NULL)
+ * receives each step's mean loss */
+int gnuts_flow_train(gnuts_model* m, gnuts_flow* f, int steps, int batch, double lr, double base_scale,
+                     unsigned int seed, double* loss_trace);
+/* hmc_nuts_diag_e_adapt (command.hpp:673-688) run on z with x = T(z): inits
+ * and the returned step size / inverse metric are in z; draws hold lp__ =
+ * the model's lp at x and write_array(x), like a plain run's */
+int gnuts_hmc_nuts_flow_diag_e_adapt(gnuts_model* m, gnuts_flow* f, const gnuts_sample_args* a,
+                                     const double* inits_z, const double* inv_metric, gnuts_output* out,
+                                     gnuts_progress_fn progress, void* ctx);
+
+typedef struct {
+  int layers, hidden;       /* default 8, 128 */
+  double clamp;             /* default 6 */
+  int train_steps, batch;   /* default 2000, 256 */
+  double learning_rate;     /* default 2e-3 */
+  double base_scale;        /* training base draws N(0, base_scale^2 I), default 1.25 */
+  int flow_warmup;          /* z-space warmup iterations, default 300 */
+  int pilot_samples;        /* draws per chain each sampler produces for the judge, default 200 */
+  double moment_tolerance;  /* combined MCSE, default 4 */
+} gnuts_learned_args;
+void gnuts_learned_args_default(gnuts_learned_args* la);
+
+typedef struct {
+  int used_flow;                    /* 1: the learned map produced the draws; 0: plain fallback */
+  double plain_ess_per_grad, flow_ess_per_grad;  /* min bulk ESS / sampling gradients, pilots */
+  double plain_divergence_rate, flow_divergence_rate;
+  double max_moment_z;              /* max over parameters |mean_f - mean_p| / sqrt(mcse_f^2 + mcse_p^2) */
+  double loss_first, loss_last;     /* mean training loss of the first / last 10 steps */
+  double plain_seconds, train_seconds, flow_seconds, final_seconds;
+  int64_t plain_grads, flow_grads, final_grads;
+} gnuts_learned_report;
+
+/* Learned-preconditioner variant of hmc_nuts_diag_e_adapt (command.hpp:
+ * 673-688): (1) plain diag_e NUTS, num_warmup adaptive iterations and
+ * pilot_samples draws; (2) flow initialised from those chains (mean of the
+ * final positions, scale from the adapted inverse metric) and trained by
+ * reverse KL through the model's own gradient kernels; (3) NUTS on z with
+ * flow_warmup adaptive iterations and pilot_samples draws; (4) the judge
+ * keeps the flow only if its ESS per gradient is not lower, its divergence
+ * rate not higher and (when the plain pilot is free of divergences) every
+ * posterior mean agrees within moment_tolerance combined MCSE; (5) the kept
+ * sampler continues, non-adapting, for num_samples draws into out. */
+int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* m, const gnuts_sample_args* a, const gnuts_learned_args* la,
+                                        const double* inits, gnuts_output* out, gnuts_learned_report* report,
+                                        gnuts_progress_fn progress, void* ctx);
+
 /* Message of the last failing call on this thread. */
 int gnuts_last_error(char* buf, size_t len);
 /* Library version string, e.g. "gnuts 0.1 (sm_103a)". */

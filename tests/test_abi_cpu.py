@@ -101,3 +101,19 @@ def test_no_gpu_fails_loudly():
     with pytest.raises(gn.GnutsError) as e:
         m.sample(num_warmup=10, num_samples=10)
     assert e.value.code == gnuts.ERR_CUDA
+
+
+def test_posterior_set_model_layout():
+    """A posterior set is built on the host: shared parameters first, alpha
+    columns up to the largest posterior."""
+    from cmdstan_gb300 import workloads
+    d = workloads.varint_set(seed=3, P=5, Jmax=30)
+    m = gn.Model("varint_set", d)
+    assert m.dim == int(d["J"].max()) + 12
+    assert m.param_names[:12] == ["beta.%d" % k for k in range(1, 11)] + ["sigma_y", "tau"]
+    assert m.param_names[12:] == ["alpha.%d" % j for j in range(1, int(d["J"].max()) + 1)]
+    bad = dict(d)
+    bad["group"] = d["group"].copy()
+    bad["group"][0] = 1000
+    with pytest.raises(gn.GnutsError):
+        gn.Model("varint_set", bad)

@@ -86,3 +86,16 @@ def test_adam_closed_form():
     oracle.adam(th, m, v, g2, 2, lr=0.01)
     step = 0.01 * (m_ref / (1 - 0.9 ** 2)) / (np.sqrt(v_ref / (1 - 0.999 ** 2)) + 1e-8)
     assert np.allclose(th, th1 - step, rtol=1e-12, atol=1e-14)
+
+
+def test_device_flow_layout_matches_oracle_without_gpu():
+    """Creating a flow is host-only: its parameter count equals the oracle's."""
+    import cmdstan_gb300 as gn
+    for d, L, H in [(2, 8, 32), (66, 8, 128), (101, 8, 128), (128, 16, 64)]:
+        assert gn.Flow(d, layers=L, hidden=H).n_params == oracle.OracleFlow(d, L, H).n_params
+    with pytest.raises(gn.GnutsError):
+        gn.Flow(1)
+    with pytest.raises(gn.GnutsError):
+        gn.Flow(129)
+    with pytest.raises(gn.GnutsError):
+        gn.Flow(10, hidden=100)

@@ -3,5 +3,5 @@
 The compute path is the CUDA library ``_lib/libgnuts.so`` (include/gnuts.h);
 ``gnuts`` is its Python mirror.
 """
-from .gnuts import (Model, Fit, Flow, GnutsError, default_args, learned_args, load, summary,  # noqa: F401
+from .gnuts import (Model, Fit, Flow, GnutsError, default_args, learned_args, train_args, load, summary,  # noqa: F401
                     summary_columns, SAMPLER_COLUMNS, METRICS, PRECISION_FP64, PRECISION_MIXED)

@@ -40,6 +40,7 @@ struct FlowIO {
   uint32_t seed;     // base draws: Philox(seed, point, stream 2, step * ceil(d/2) + i/2)
   int step;
   float base_scale;  // base draws are base_scale * N(0, 1)
+  double beta;       // TRAIN: objective beta * lp_x + log|det| (tempered target while annealing)
   int jac;
   int with_model;    // FM_FWD: evaluate the model at x as well
   double* x;         // [n][d] T(z) (may be null)
@@ -354,6 +355,11 @@ __global__ void __launch_bounds__(128) k_flow(FlowDev F, DevModel M, FlowIO io) 
           __syncwarp();
           lpx = warp_log_prob_grad(M, x, gx, io.jac, lane);
           __syncwarp();
+          if (MODE == FM_TRAIN && io.beta != 1.0) {
+            lpx *= io.beta;
+            for (int i = lane; i < d; i += 32) gx[i] *= io.beta;
+            __syncwarp();
+          }
           lp = lpx + wsum(ld);
           for (int i = lane; i < d; i += 32) yb[i] = (float)(gx[i] * exp((double)rho[i]));
           __syncwarp();
@@ -874,6 +880,7 @@ int flow_log_prob_grad(Model& m, Flow& f, int n, const double* z, int jacobian, 
   io.loss = loss.p;
   io.valid = valid.p;
   io.nvalid = f.nvalid;
+  io.beta = 1.0;
   if ((rc = configure_flow(f, err)) || (rc = launch_flow(f, m.dev, FM_TRAIN, io, 0, err))) return rc;
   if (grad_theta) {
     const FlowDev F = dev_of(f);
@@ -904,8 +911,9 @@ int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, dou
   return GNUTS_OK;
 }
 
-int flow_train(Model& m, Flow& f, int steps, int batch, double lr, double base_scale, unsigned seed,
-               double* loss_trace, std::string& err) {
+int flow_train(Model& m, Flow& f, const gnuts_train_args& ta, double* loss_trace, std::string& err) {
+  const int steps = ta.steps, batch = ta.batch;
+  const double lr = ta.learning_rate;
   int rc = upload(m, err);
   if (rc) return rc;
   if (m.dev.D != f.d) {
@@ -924,8 +932,8 @@ int flow_train(Model& m, Flow& f, int steps, int batch, double lr, double base_s
   const FlowDev F = dev_of(f);
   FlowIO io{};
   io.n = batch;
-  io.seed = seed;
-  io.base_scale = (float)base_scale;
+  io.seed = ta.seed;
+  io.base_scale = (float)ta.base_scale;
   io.jac = 1;
   io.fac = fac.p;
   io.loss = loss.p;
@@ -936,6 +944,10 @@ int flow_train(Model& m, Flow& f, int steps, int batch, double lr, double base_s
   for (int t = 1; t <= steps; ++t) {
     FL_CUDA(cudaMemsetAsync(f.nvalid, 0, sizeof(int)));
     io.step = t - 1;
+    // tempered target beta * lp_x, beta rising linearly from beta0 to 1 over
+    // the first anneal_fraction of the steps
+    const double ramp = ta.anneal_fraction > 0 ? (double)(t - 1) / (ta.anneal_fraction * steps) : 1.0;
+    io.beta = ramp >= 1.0 ? 1.0 : ta.beta0 + (1.0 - ta.beta0) * ramp;
     if ((rc = launch_flow(f, m.dev, FM_TRAIN, io, 0, err))) return rc;
     k_flow_pgrad<<<pblocks, 256>>>(F, batch, fac.p, valid.p, f.grad);
     // learning rate decays linearly to a tenth of its start over the run

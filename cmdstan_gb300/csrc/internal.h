@@ -116,8 +116,7 @@ int flow_log_prob_grad(Model& m, Flow& f, int n, const double* z, int jacobian, 
                        double* grad_theta, std::string& err);
 int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, double b2, double eps,
                    std::string& err);
-int flow_train(Model& m, Flow& f, int steps, int batch, double lr, double base_scale, unsigned seed,
-               double* loss_trace, std::string& err);
+int flow_train(Model& m, Flow& f, const gnuts_train_args& ta, double* loss_trace, std::string& err);
 // noalloc.cu: the allocation-free batched gradient (device pointers)
 int noalloc_log_prob_grad(const Model& m, int n, const double* q, int jac, double* lp, double* g, std::string& err);
 

@@ -181,13 +181,31 @@ int gnuts_flow_adam_step(gnuts_flow* f, const double* grad, int t, double lr, do
   return rc ? api_fail(rc, err) : GNUTS_OK;
 }
 
-int gnuts_flow_train(gnuts_model* m, gnuts_flow* f, int steps, int batch, double lr, double base_scale,
-                     unsigned int seed, double* loss_trace) {
-  if (!m || !f) return api_fail(GNUTS_ERR_ARGUMENT, "null argument");
-  if (steps < 0 || batch < 1 || batch > 65536 || !(lr > 0) || !(base_scale > 0))
-    return api_fail(GNUTS_ERR_ARGUMENT, "training needs steps >= 0, 1 <= batch <= 65536, lr > 0, base_scale > 0");
+void gnuts_train_args_default(gnuts_train_args* ta) {
+  if (!ta) return;
+  ta->steps = 2000;
+  ta->batch = 256;
+  ta->learning_rate = 2e-3;
+  ta->base_scale = 1.25;
+  ta->beta0 = 0.3;
+  ta->anneal_fraction = 0.5;
+  ta->seed = 0;
+}
+
+static int check_train_args(const gnuts_train_args& t) {
+  if (t.steps < 0 || t.batch < 1 || t.batch > 65536 || !(t.learning_rate > 0) || !(t.base_scale > 0) ||
+      !(t.beta0 > 0 && t.beta0 <= 1) || !(t.anneal_fraction >= 0 && t.anneal_fraction <= 1))
+    return api_fail(GNUTS_ERR_ARGUMENT, "training needs steps >= 0, 1 <= batch <= 65536, learning_rate > 0, "
+                                        "base_scale > 0, 0 < beta0 <= 1, 0 <= anneal_fraction <= 1");
+  return GNUTS_OK;
+}
+
+int gnuts_flow_train(gnuts_model* m, gnuts_flow* f, const gnuts_train_args* ta, double* loss_trace) {
+  if (!m || !f || !ta) return api_fail(GNUTS_ERR_ARGUMENT, "null argument");
+  int rc = check_train_args(*ta);
+  if (rc) return rc;
   std::string err;
-  int rc = flow_train(*Mo(m), *F(f), steps, batch, lr, base_scale, seed, loss_trace, err);
+  rc = flow_train(*Mo(m), *F(f), *ta, loss_trace, err);
   return rc ? api_fail(rc, err) : GNUTS_OK;
 }
 
@@ -212,10 +230,7 @@ void gnuts_learned_args_default(gnuts_learned_args* la) {
   la->layers = 8;
   la->hidden = 128;
   la->clamp = 6.0;
-  la->train_steps = 2000;
-  la->batch = 256;
-  la->learning_rate = 2e-3;
-  la->base_scale = 1.25;
+  gnuts_train_args_default(&la->train);
   la->flow_warmup = 300;
   la->pilot_samples = 200;
   la->moment_tolerance = 4.0;
@@ -228,10 +243,9 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   Model& m = *Mo(mh);
   int rc = validate_args(m, a, 1, 0);
   if (rc) return rc;
-  if (la->pilot_samples < 20 || la->flow_warmup < 20 || la->train_steps < 0 || la->batch < 1 ||
-      !(la->base_scale > 0) || !(la->learning_rate > 0))
-    return api_fail(GNUTS_ERR_ARGUMENT,
-                    "learned sampler needs pilot_samples >= 20, flow_warmup >= 20, batch >= 1, base_scale > 0");
+  if (la->pilot_samples < 20 || la->flow_warmup < 20)
+    return api_fail(GNUTS_ERR_ARGUMENT, "learned sampler needs pilot_samples >= 20 and flow_warmup >= 20");
+  if ((rc = check_train_args(la->train))) return rc;
   const int C = a->num_chains, D = m.dev.D, ncol = 7 + m.dev.ncon, P = la->pilot_samples;
   if (D < 2) return api_fail(GNUTS_ERR_ARGUMENT, "the learned map needs at least 2 parameters");
   std::string err;
@@ -269,16 +283,19 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   for (int i = 0; i < D; ++i) scale[i] = std::sqrt(std::max(scale[i], 1e-12));
   rc = gnuts_flow_init_affine(reinterpret_cast<gnuts_flow*>(fl), mean.data(), scale.data(), a->seed + 1u, 0.5);
   if (rc) return rc;
-  std::vector<double> trace(std::max(1, la->train_steps));
-  rc = flow_train(m, *fl, la->train_steps, la->batch, la->learning_rate, la->base_scale, a->seed + 1u,
+  const int steps = la->train.steps;
+  std::vector<double> trace(std::max(1, steps));
+  gnuts_train_args ta = la->train;
+  ta.seed = a->seed + 1u;
+  rc = flow_train(m, *fl, ta,
                   trace.data(), err);
   if (rc) return api_fail(rc, err);
   rep.train_seconds = now_s() - t0;
-  if (la->train_steps > 0) {
-    const int k = std::min(10, la->train_steps);
+  if (steps > 0) {
+    const int k = std::min(10, steps);
     for (int i = 0; i < k; ++i) {
       rep.loss_first += trace[i] / k;
-      rep.loss_last += trace[la->train_steps - 1 - i] / k;
+      rep.loss_last += trace[steps - 1 - i] / k;
     }
   }
 

@@ -35,7 +35,7 @@ EXPORTS = [
     "gnuts_flow_create", "gnuts_flow_destroy", "gnuts_flow_num_params", "gnuts_flow_set_params",
     "gnuts_flow_get_params", "gnuts_flow_init_affine", "gnuts_flow_forward", "gnuts_flow_inverse",
     "gnuts_flow_log_prob_grad", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
-    "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt",
+    "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt", "gnuts_train_args_default",
 ]
 SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
 
@@ -104,10 +104,15 @@ class Output(ctypes.Structure):
                 ("timing", ctypes.c_void_p)]
 
 
+class TrainArgs(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("batch", ctypes.c_int), ("learning_rate", ctypes.c_double),
+                ("base_scale", ctypes.c_double), ("beta0", ctypes.c_double), ("anneal_fraction", ctypes.c_double),
+                ("seed", ctypes.c_uint)]
+
+
 class LearnedArgs(ctypes.Structure):
     _fields_ = [("layers", ctypes.c_int), ("hidden", ctypes.c_int), ("clamp", ctypes.c_double),
-                ("train_steps", ctypes.c_int), ("batch", ctypes.c_int), ("learning_rate", ctypes.c_double),
-                ("base_scale", ctypes.c_double), ("flow_warmup", ctypes.c_int), ("pilot_samples", ctypes.c_int),
+                ("train", TrainArgs), ("flow_warmup", ctypes.c_int), ("pilot_samples", ctypes.c_int),
                 ("moment_tolerance", ctypes.c_double)]
 
 
@@ -182,7 +187,9 @@ def load():
     lib.gnuts_flow_inverse.argtypes = [vp, ip, dp, dp, dp]
     lib.gnuts_flow_log_prob_grad.argtypes = [vp, vp, ip, dp, ip, dp, dp, dp]
     lib.gnuts_flow_adam_step.argtypes = [vp, dp, ip] + [ctypes.c_double] * 4
-    lib.gnuts_flow_train.argtypes = [vp, vp, ip, ip, ctypes.c_double, ctypes.c_double, ctypes.c_uint, dp]
+    lib.gnuts_train_args_default.argtypes = [ctypes.POINTER(TrainArgs)]
+    lib.gnuts_train_args_default.restype = None
+    lib.gnuts_flow_train.argtypes = [vp, vp, ctypes.POINTER(TrainArgs), dp]
     lib.gnuts_hmc_nuts_flow_diag_e_adapt.argtypes = [vp, vp, ctypes.POINTER(SampleArgs), dp, dp,
                                                      ctypes.POINTER(Output), PROGRESS_FN, vp]
     lib.gnuts_learned_args_default.argtypes = [ctypes.POINTER(LearnedArgs)]
@@ -401,13 +408,28 @@ class Model:
         return qo, st, ctr
 
 
-def learned_args(**kw):
+def train_args(**kw):
+    ta = TrainArgs()
+    load().gnuts_train_args_default(ctypes.byref(ta))
+    for k, v in kw.items():
+        if not hasattr(ta, k):
+            raise TypeError("unknown training argument %r" % k)
+        setattr(ta, k, v)
+    return ta
+
+
+def learned_args(train=None, **kw):
+    """Learned-sampler arguments; `train` is a dict of gnuts_train_args fields."""
     la = LearnedArgs()
     load().gnuts_learned_args_default(ctypes.byref(la))
     for k, v in kw.items():
-        if not hasattr(la, k):
+        if not hasattr(la, k) or k == "train":
             raise TypeError("unknown learned-sampler argument %r" % k)
         setattr(la, k, v)
+    for k, v in (train or {}).items():
+        if not hasattr(la.train, k):
+            raise TypeError("unknown training argument %r" % k)
+        setattr(la.train, k, v)
     return la
 
 
@@ -468,7 +490,9 @@ class Flow:
         g = np.ascontiguousarray(grad, dtype=np.float64)
         _check(self._lib.gnuts_flow_adam_step(self._h, _dp(g), int(t), lr, beta1, beta2, eps))
 
-    def train(self, model, steps, batch=256, lr=2e-3, seed=0, base_scale=1.0):
+    def train(self, model, steps, **kw):
+        """Reverse-KL training (gnuts_train_args fields as keywords); returns the loss trace."""
+        ta = train_args(steps=steps, **kw)
         trace = np.zeros(max(1, steps))
-        _check(self._lib.gnuts_flow_train(model._h, self._h, steps, batch, lr, float(base_scale), seed, _dp(trace)))
+        _check(self._lib.gnuts_flow_train(model._h, self._h, ctypes.byref(ta), _dp(trace)))
         return trace[:steps]

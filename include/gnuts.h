@@ -238,15 +238,27 @@ int gnuts_flow_log_prob_grad(gnuts_model* m, gnuts_flow* f, int n, const double*
 /* one Adam step (bias-corrected, step t >= 1) with the given gradient */
 int gnuts_flow_adam_step(gnuts_flow* f, const double* grad, int t, double lr, double beta1, double beta2,
                          double eps);
-/* reverse-KL training: each step draws `batch` base points
- * z ~ N(0, base_scale^2 I) (Philox stream 2 of (seed, point)) and minimises
- * the mean of -(lp_x(T(z)) + log|det|) with Adam (0.9, 0.999, 1e-8; learning
- * rate decaying linearly from lr to lr / 10).  The minimiser pulls the
- * posterior back to N(0, base_scale^2 I): base_scale 1 is the reverse KL;
- * larger values weight the tails more.  loss_trace (steps, may be NULL)
- * receives each step's mean loss */
-int gnuts_flow_train(gnuts_model* m, gnuts_flow* f, int steps, int batch, double lr, double base_scale,
-                     unsigned int seed, double* loss_trace);
+/* Reverse-KL training.  Each step draws `batch` base points
+ * z ~ N(0, base_scale^2 I) (Philox stream 2 of (seed, point)) and takes one
+ * Adam step (0.9, 0.999, 1e-8; learning rate decaying linearly from
+ * learning_rate to a tenth of it) on the mean of
+ * -(beta * lp_x(T(z)) + log|det|).  beta rises linearly from beta0 to 1 over
+ * the first anneal_fraction of the steps (a tempered, wider target first, so
+ * the map does not collapse onto one region), then stays 1.  At beta = 1 the
+ * minimiser pulls the posterior back to N(0, base_scale^2 I): base_scale 1 is
+ * the reverse KL; larger values weight the tails more. */
+typedef struct {
+  int steps, batch;         /* default 2000, 256 */
+  double learning_rate;     /* default 2e-3 */
+  double base_scale;        /* default 1.25 */
+  double beta0;             /* default 0.3 */
+  double anneal_fraction;   /* default 0.5 (0: no annealing) */
+  unsigned int seed;
+} gnuts_train_args;
+void gnuts_train_args_default(gnuts_train_args* ta);
+/* loss_trace (steps, may be NULL) receives each step's mean loss */
+int gnuts_flow_train(gnuts_model* m, gnuts_flow* f, const gnuts_train_args* ta, double* loss_trace);
+
 /* hmc_nuts_diag_e_adapt (command.hpp:673-688) run on z with x = T(z): inits
  * and the returned step size / inverse metric are in z; draws hold lp__ =
  * the model's lp at x and write_array(x), like a plain run's */
@@ -257,9 +269,7 @@ int gnuts_hmc_nuts_flow_diag_e_adapt(gnuts_model* m, gnuts_flow* f, const gnuts_
 typedef struct {
   int layers, hidden;       /* default 8, 128 */
   double clamp;             /* default 6 */
-  int train_steps, batch;   /* default 2000, 256 */
-  double learning_rate;     /* default 2e-3 */
-  double base_scale;        /* training base draws N(0, base_scale^2 I), default 1.25 */
+  gnuts_train_args train;   /* gnuts_train_args_default; the seed is derived from the sampler's */
   int flow_warmup;          /* z-space warmup iterations, default 300 */
   int pilot_samples;        /* draws per chain each sampler produces for the judge, default 200 */
   double moment_tolerance;  /* combined MCSE, default 4 */

@@ -115,7 +115,7 @@ def test_training_reduces_reverse_kl_on_funnel():
     f = gn.Flow(m.dim, layers=8, hidden=128)
     scale = np.r_[3.0, np.full(100, 2.0)]
     f.init_affine(np.zeros(m.dim), scale, seed=1)
-    trace = f.train(m, steps=400, batch=256, lr=2e-3, seed=7)
+    trace = f.train(m, steps=400, batch=256, learning_rate=2e-3, seed=7, base_scale=1.0, anneal_fraction=0.0)
     assert np.all(np.isfinite(trace))
     first, last = trace[:20].mean(), trace[-20:].mean()
     assert last < first - 5.0, (first, last)
@@ -129,7 +129,8 @@ def test_flow_sampler_is_exact_on_gaussian():
     m = gn.Model("normal", {"scales": scales})
     of = oracle.OracleFlow(6, layers=4, hidden=32, clamp=2.0)
     f = gn.Flow(6, layers=4, hidden=32, clamp=2.0)
-    th = _random_theta(of, rng, w2=0.15, rho=0.0)
+    th = _random_theta(of, rng, w2=0.05, rho=0.0)
+    th[-6:] = np.log(scales)  # x = scale * u: the couplings perturb a unit-scale target
     f.set_params(th)
     fit = m.sample_flow(f, num_chains=64, num_warmup=400, num_samples=400, seed=3)
     assert np.all(fit.status == 0)
@@ -138,7 +139,7 @@ def test_flow_sampler_is_exact_on_gaussian():
         st = gn.summary(x)
         assert abs(st["mean"]) < 4.5 * st["mcse"] + 1e-12, (k, st)
         assert abs(st["sd"] / s - 1) < 0.08, (k, st["sd"], s)
-        assert st["rhat"] < 1.1
+        assert st["rhat"] < 1.05
     # lp__ is the model's lp at x: -0.5 sum (x/s)^2
     xs = fit.draws[:, :, 7:]
     assert np.allclose(fit.draws[:, :, 0], -0.5 * ((xs / scales) ** 2).sum(axis=2), rtol=1e-9, atol=1e-9)
@@ -164,7 +165,7 @@ def test_learned_sampler_beats_plain_on_funnel():
 def test_learned_judge_applies_its_rule():
     m = gn.Model("hier", workloads.eight_schools())
     fit, rep = m.sample_learned(num_chains=32, num_warmup=300, num_samples=100, seed=4,
-                                learned=dict(train_steps=100, pilot_samples=60, flow_warmup=60, hidden=32,
+                                learned=dict(train=dict(steps=100), pilot_samples=60, flow_warmup=60, hidden=32,
                                              layers=4))
     clean = rep["plain_divergence_rate"] <= 1e-3
     expect = (rep["flow_ess_per_grad"] >= rep["plain_ess_per_grad"]

@@ -224,7 +224,10 @@ def bench_varint_set(peaks):
     # FP32 X row (K floats) + FP64 y per row and gradient
     algo_bytes = float((lf * rows).sum() * (4 * d["K"] + 8))
     ess, rhat = _min_ess_rhat(fit.draws, [(4, int(j) + 12) for j in d["J"]])
-    return {"workload": "512 varying-intercept regressions, J log-uniform [8,256], n_j ~ Poisson(50)+5, K=10, "
+    cpu = _oracle_rate("varint", workloads.varint_set_member(d, int(np.argsort(d["N"])[len(d["N"]) // 2])), 16, 5.0)
+    cpu["sample"] = "the median-size posterior: " + cpu["sample"]
+    return {"cpu_baseline": cpu,
+            "workload": "512 varying-intercept regressions, J log-uniform [8,256], n_j ~ Poisson(50)+5, K=10, "
                         "4 chains each (2048 chains) in one launch, 1000 warmup + 1000 draws, FP32 rows / FP64 energy",
             "grad_evals_per_s": float(lf.sum() / dev_s), "min_bulk_ess_per_s": ess / dev_s, "min_bulk_ess": ess,
             "rhat_max": rhat, "device_s": dev_s, "wall_s": wall, "rows_total": int(d["N"].sum()),
@@ -232,6 +235,69 @@ def bench_varint_set(peaks):
                          "unit": "GB/s", "frac": algo_bytes / dev_s / 1e9 / float(peaks["hbm_gbs"]),
                          "note": "algorithmic row bytes (4K + 8 per row per gradient) over the run's device time; "
                                  "the 99.5 MB of rows stay L2-resident, so the bound is latency, not HBM"}}
+
+
+def _oracle_rate(model_id, data, chains, seconds, **kw):
+    """CPU oracle NUTS on the host cores (one chain per core): grad-evals/s of a
+    bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = os.cpu_count() or 1
+    om = oracle.OracleModel(model_id, data)
+    n = max(1, min(chains, threads))
+    t = time.time()
+    _, _, _, ng = om.run_chains(n, threads=threads, num_warmup=kw.get("probe_warmup", 20), num_samples=1, seed=5)
+    per = max((time.time() - t) / (kw.get("probe_warmup", 20) + 1), 1e-6)
+    iters = int(max(2, min(100000, seconds / per)))
+    wu = iters // 2
+    t = time.time()
+    _, _, _, ng = om.run_chains(n, threads=threads, num_warmup=wu, num_samples=iters - wu, seed=5)
+    wall = time.time() - t
+    return {"value": float(ng.sum() / wall), "unit": "grad-evals/s", "cores": threads, "kind": "port",
+            "sample": "%d chains x %d iterations (%d adaptive warmup) of the same model, FP64, %.1f s" %
+                      (n, iters, wu, wall)}
+
+
+def bench_bernoulli():
+    """Bernoulli example (N = 10, y ~ Bernoulli(0.2)), 4 chains x 1000 + 1000, FP64."""
+    import cmdstan_gb300 as gn
+    from cmdstan_gb300 import workloads
+    d = workloads.bernoulli(seed=0)
+    m = gn.Model("bernoulli", d)
+    m.sample(num_chains=4, num_warmup=50, num_samples=50, seed=1, refresh=0)
+    t0 = time.perf_counter()
+    fit = m.sample(num_chains=4, num_warmup=NUM_WARMUP, num_samples=NUM_SAMPLES, seed=2, refresh=0)
+    wall = time.perf_counter() - t0
+    ess, rhat = _min_ess_rhat(fit.draws)
+    return {"workload": "bernoulli N=10, 4 chains, 1000 warmup + 1000 draws, FP64",
+            "grad_evals_per_s": float(fit.n_leapfrog.sum() / wall), "min_bulk_ess_per_s": ess / wall,
+            "min_bulk_ess": ess, "rhat_max": rhat, "wall_s": wall,
+            "cpu_baseline": _oracle_rate("bernoulli", d, 4, 3.0, probe_warmup=200)}
+
+
+def bench_horseshoe_gradient(chains=256):
+    """Regularised-horseshoe logistic regression, X 200,000 x 1000 (BF16-exact),
+    batched gradient of 256 chains (FP32 CUDA-core contraction, FP64 priors and
+    lp sum): gradient evaluations per second; the 2003-dimensional sampler run
+    itself is not part of the bench."""
+    import cmdstan_gb300 as gn
+    from cmdstan_gb300 import workloads
+    d = workloads.horseshoe(seed=0)
+    m = gn.Model("horseshoe", d)
+    rng = np.random.default_rng(3)
+    q = rng.normal(0, 0.1, (chains, m.dim))
+    m.log_prob_grad(q, precision=gn.PRECISION_MIXED)
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        m.log_prob_grad(q, precision=gn.PRECISION_MIXED)
+    wall = (time.perf_counter() - t0) / reps
+    N, K = d["X"].shape
+    return {"workload": "horseshoe logistic N=200000 x D=1000, %d chains, one batched gradient" % chains,
+            "grad_evals_per_s": chains / wall, "s_per_batched_gradient": wall,
+            "tflops": 4.0 * N * K * chains / wall / 1e12,
+            "note": "host round trip of q / lp / gradient included; FP32 SIMT contraction (no tensor-core path "
+                    "for K = 1000)"}
 
 
 def bench_funnel(chains=256):
@@ -251,7 +317,8 @@ def bench_funnel(chains=256):
                                refresh=0)
     tl = time.perf_counter() - t0
     el, rl = _min_ess_rhat(fl.draws)
-    return {"workload": "funnel v ~ N(0,3), x_1..100 ~ N(0, exp(v/2)); %d chains; 1000 warmup + 1000 draws" % chains,
+    return {"cpu_baseline": _oracle_rate("funnel", workloads.funnel(100), 16, 5.0),
+            "workload": "funnel v ~ N(0,3), x_1..100 ~ N(0, exp(v/2)); %d chains; 1000 warmup + 1000 draws" % chains,
             "plain": {"min_bulk_ess_per_s": ep / tp, "min_bulk_ess": ep, "rhat_max": rp, "seconds": tp,
                       "divergence_rate": float(fp.draws[:, :, 5].mean()),
                       "grad_evals": float(fp.n_leapfrog.sum())},
@@ -387,7 +454,8 @@ def main():
     if rank == 0:
         if not args.no_extra:
             extra = {}
-            for name, fn in (("varint_set_512x4", lambda: bench_varint_set(peaks)), ("funnel_100d", bench_funnel)):
+            for name, fn in (("bernoulli", bench_bernoulli), ("varint_set_512x4", lambda: bench_varint_set(peaks)),
+                             ("funnel_100d", bench_funnel), ("horseshoe_gradient", bench_horseshoe_gradient)):
                 try:
                     extra[name] = fn()
                 except Exception as e:  # reported in the line, the headline stands

@@ -31,7 +31,8 @@ struct GradOut {
   double* coef64;   // [C][K+1]
   float* coef32;    // [C][K+1]
   double* part_lp;  // [S][C]
-  double* part_g;   // [S][C][K+1]
+  double* part_g;   // [S][C][K+1] (SIMT path)
+  float* part_g32;  // [S][C][TC_GSTRIDE] (tensor-core path: FP32 accumulators)
   const int* done_count;
   int C_total;
   void* tc;           // tensor-core plan (grad_tc.cu), null for the SIMT path
@@ -76,6 +77,35 @@ __device__ __forceinline__ void sum_splits(const GradOut& G, int c, double* out,
     }
   }
 }
+// Tensor-core partials: lane l owns coefficients 4l .. 4l+3 and loads one
+// 16-byte vector per split, all splits in flight at once, summed in split
+// order in FP32 (the same values and order as the FP64-stored path).
+__device__ __forceinline__ void sum_splits_f32(const GradOut& G, int c, double* out, int lane) {
+  const float4* src = reinterpret_cast<const float4*>(G.part_g32 + (size_t)c * TC_GSTRIDE) + lane;
+  const size_t stride = (size_t)G.C * TC_GSTRIDE / 4;
+  constexpr int SB = 16;  // splits loaded together
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int s0 = 0; s0 < G.S; s0 += SB) {
+    float4 v[SB];
+#pragma unroll
+    for (int u = 0; u < SB; ++u)
+      if (s0 + u < G.S) v[u] = src[(size_t)(s0 + u) * stride];
+#pragma unroll
+    for (int u = 0; u < SB; ++u)
+      if (s0 + u < G.S) {
+        a.x += v[u].x;
+        a.y += v[u].y;
+        a.z += v[u].z;
+        a.w += v[u].w;
+      }
+  }
+  const int i = 4 * lane;
+  if (i <= G.K) out[i] = (double)a.x;
+  if (i + 1 <= G.K) out[i + 1] = (double)a.y;
+  if (i + 2 <= G.K) out[i + 2] = (double)a.z;
+  if (i + 3 <= G.K) out[i + 3] = (double)a.w;
+}
+
 // lp partials of chain c summed in FP64, same order on every lane
 __device__ __forceinline__ double sum_split_lp(const GradOut& G, int c) {
   double t = 0;
@@ -143,7 +173,8 @@ __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevMod
                                                   double* g, int lane) {
   const int K = M.K;
   // likelihood gradient wrt (b0, beta) -> g[0..K]; priors added below
-  if (G.prec == GNUTS_PRECISION_FP64) sum_splits<double>(G, c, g, lane);
+  if (G.part_g32) sum_splits_f32(G, c, g, lane);
+  else if (G.prec == GNUTS_PRECISION_FP64) sum_splits<double>(G, c, g, lane);
   else sum_splits<float>(G, c, g, lane);
   double lp = sum_split_lp(G, c);
   __syncwarp();

@@ -174,7 +174,7 @@ struct TcArgs {
   int N, K, C, Cpad, rows_per_split, S, C_total;
   const uint32_t* ybits;
   double* part_lp;
-  double* part_g;
+  float* part_g;  // [S][C][TC_GSTRIDE]: coefficient 0 = intercept, 1 + k = beta_k
   const int* done_count;
   int* error;
 };
@@ -416,17 +416,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       tmem_ld16(ta + 16, g + 16);
       tmem_wait_ld();
       if (c < A.C) {
-        double* pg = A.part_g + ((size_t)split * A.C + c) * (A.K + 1);
+        float* pg = A.part_g + ((size_t)split * A.C + c) * TC_GSTRIDE;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int k = sub * 32 + j;
-          if (k < A.K) pg[1 + k] = (double)g[j];
-          else if (k == A.K) pg[0] = (double)g[j];
+          if (k < A.K) pg[1 + k] = g[j];
+          else if (k == A.K) pg[0] = g[j];
         }
       }
     } else if (T == 0 && c < A.C) {
-      double* pg = A.part_g + ((size_t)split * A.C + c) * (A.K + 1);
-      for (int k = sub; k <= A.K; k += 4) pg[k] = 0.0;
+      float* pg = A.part_g + ((size_t)split * A.C + c) * TC_GSTRIDE;
+      for (int k = sub; k <= A.K; k += 4) pg[k] = 0.f;
     }
     lpx[sub * 128 + cl] = lp_acc;
     asm volatile("bar.sync 1, 512;" ::: "memory");
@@ -487,13 +487,13 @@ struct TcPlan {
   uint16_t* coef = nullptr;
   int* error = nullptr;
   double* part_lp = nullptr;
-  double* part_g = nullptr;
+  float* part_g = nullptr;
 };
 
 bool tc_supported(const DevModel& M) { return M.kind == MK_LOGISTIC && M.Xtc && M.K + 1 <= XTC_LD; }
 
 int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uint16_t** coef_bf, int* S_out,
-              double** part_lp, double** part_g, std::string& err) {
+              double** part_lp, float** part_g, std::string& err) {
   if (!tc_supported(M)) {
     err = "tensor-core gradient needs a logistic model with at most 103 predictors";
     return GNUTS_ERR_ARGUMENT;
@@ -519,7 +519,10 @@ int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uin
   if ((e = cudaMalloc(&p->error, sizeof(int))) != cudaSuccess) return fail(e);
   cudaMemset(p->error, 0, sizeof(int));
   if ((e = cudaMalloc(&p->part_lp, sizeof(double) * S * C)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&p->part_g, sizeof(double) * S * C * (M.K + 1))) != cudaSuccess) return fail(e);
+  // padded to TC_GSTRIDE floats per chain (entries past K stay zero) so the
+  // consumer sums whole 16-byte vectors
+  if ((e = cudaMalloc(&p->part_g, sizeof(float) * S * C * TC_GSTRIDE)) != cudaSuccess) return fail(e);
+  cudaMemset(p->part_g, 0, sizeof(float) * S * C * TC_GSTRIDE);
   int rc = make_map(&p->xmap, M.Xtc, XTC_LD, (uint64_t)M.N, XTC_LD * 2, err);
   if (!rc) rc = make_map(&p->cmap, p->coef, 128, (uint64_t)2 * Cpad, 256, err);
   if (rc) {

@@ -10,10 +10,10 @@ struct TcPlan;  // tensor maps, buffers, launch shape
 
 // Builds the plan for C chains of a logistic model with K + 1 <= 128.
 // coef_bf (returned) is the [2][Cpad][128] BF16 hi/lo coefficient buffer that
-// stage_request fills; part_lp / part_g follow the [S][C] / [S][C][K+1]
-// layout of the batched reduction.
+// stage_request fills; part_lp is [S][C] FP64, part_g [S][C][TC_GSTRIDE] FP32
+// (the TMEM accumulators as they are).
 int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** plan, uint16_t** coef_bf, int* S,
-              double** part_lp, double** part_g, std::string& err);
+              double** part_lp, float** part_g, std::string& err);
 void tc_destroy(TcPlan* plan);
 bool tc_supported(const DevModel& M);
 void tc_launch(const TcPlan* plan, cudaStream_t stream);

@@ -49,6 +49,7 @@ struct DevModel {
   int n_members;
 };
 constexpr int XTC_LD = 104;  // row stride in elements (208 B, a multiple of 16 B)
+constexpr int TC_GSTRIDE = 128;  // FP32 gradient partials per chain of the tensor-core path
 
 struct Model {
   std::string id, name;

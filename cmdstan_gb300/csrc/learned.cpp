@@ -187,8 +187,8 @@ void gnuts_train_args_default(gnuts_train_args* ta) {
   ta->batch = 256;
   ta->learning_rate = 2e-3;
   ta->base_scale = 1.25;
-  ta->beta0 = 0.3;
-  ta->anneal_fraction = 0.5;
+  ta->beta0 = 1.0;
+  ta->anneal_fraction = 0.0;
   ta->seed = 0;
 }
 
@@ -232,6 +232,7 @@ void gnuts_learned_args_default(gnuts_learned_args* la) {
   la->clamp = 6.0;
   gnuts_train_args_default(&la->train);
   la->flow_warmup = 300;
+  la->flow_delta = 0.95;
   la->pilot_samples = 200;
   la->moment_tolerance = 4.0;
 }
@@ -243,8 +244,9 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   Model& m = *Mo(mh);
   int rc = validate_args(m, a, 1, 0);
   if (rc) return rc;
-  if (la->pilot_samples < 20 || la->flow_warmup < 20)
-    return api_fail(GNUTS_ERR_ARGUMENT, "learned sampler needs pilot_samples >= 20 and flow_warmup >= 20");
+  if (la->pilot_samples < 20 || la->flow_warmup < 20 || !(la->flow_delta > 0 && la->flow_delta < 1))
+    return api_fail(GNUTS_ERR_ARGUMENT,
+                    "learned sampler needs pilot_samples >= 20, flow_warmup >= 20 and 0 < flow_delta < 1");
   if ((rc = check_train_args(la->train))) return rc;
   const int C = a->num_chains, D = m.dev.D, ncol = 7 + m.dev.ncon, P = la->pilot_samples;
   if (D < 2) return api_fail(GNUTS_ERR_ARGUMENT, "the learned map needs at least 2 parameters");
@@ -272,15 +274,28 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   rep.plain_seconds = now_s() - t0;
   for (int c = 0; c < C; ++c) rep.plain_grads += rp.nlf[c];
 
-  // (2) flow start from the plain chains, then reverse-KL training
+  // (2) flow start from the plain chains, then reverse-KL training.  The
+  // affine part starts at the median and the MAD-based scale of the chains'
+  // final positions, pooled across chains: chains that each cover only part
+  // of the posterior (a funnel's chains stuck at different v) still spread
+  // across it together, and the median / MAD ignore the few far-out ones.
   t0 = now_s();
   std::vector<double> mean(D, 0.0), scale(D, 0.0);
-  for (int c = 0; c < C; ++c)
+  {
+    std::vector<double> col(C);
     for (int i = 0; i < D; ++i) {
-      mean[i] += q_plain[(size_t)c * D + i] / C;
-      scale[i] += rp.minv[(size_t)c * D + i] / C;
+      for (int c = 0; c < C; ++c) col[c] = q_plain[(size_t)c * D + i];
+      std::sort(col.begin(), col.end());
+      const double med = C % 2 ? col[C / 2] : 0.5 * (col[C / 2 - 1] + col[C / 2]);
+      for (int c = 0; c < C; ++c) col[c] = std::fabs(col[c] - med);
+      std::sort(col.begin(), col.end());
+      const double mad = C % 2 ? col[C / 2] : 0.5 * (col[C / 2 - 1] + col[C / 2]);
+      double ms = 0;  // fallback: the adapted metric (within-chain scale)
+      for (int c = 0; c < C; ++c) ms += rp.minv[(size_t)c * D + i] / C;
+      mean[i] = med;
+      scale[i] = mad > 0 ? 1.4826 * mad : std::sqrt(std::max(ms, 1e-12));
     }
-  for (int i = 0; i < D; ++i) scale[i] = std::sqrt(std::max(scale[i], 1e-12));
+  }
   rc = gnuts_flow_init_affine(reinterpret_cast<gnuts_flow*>(fl), mean.data(), scale.data(), a->seed + 1u, 0.5);
   if (rc) return rc;
   const int steps = la->train.steps;
@@ -312,6 +327,7 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   af.save_warmup = 0;
   af.thin = 1;
   af.seed = a->seed + 2u;
+  af.delta = la->flow_delta;
   RunBufs rf(C, P, ncol, D);
   std::vector<double> z_flow((size_t)C * D);
   {

@@ -398,7 +398,7 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   G.K = M.K;
   G.done_count = done_count;
   if (prec == GNUTS_PRECISION_MIXED && tc_supported(M)) {
-    int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g, err);
+    int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g32, err);
     if (st) return st;
     G.tc = gs.plan;
     G.Cpad = (C + 127) / 128 * 128;
@@ -625,12 +625,16 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   P.replay = p0 != nullptr;
   P.n_saved = (a.save_warmup ? (a.num_warmup + a.thin - 1) / a.thin : 0) + (a.num_samples + a.thin - 1) / a.thin;
   P.grad_budget = 2048;
-  // cache the chain vectors in shared memory when four chains fit in a block's budget
+  // cache the chain vectors in shared memory when four chains fit in a block's
+  // budget.  It pays where a launch runs many steps of a chain (fused mode);
+  // in round mode a launch runs one step and the copy in / out costs what it
+  // saves (measured on the logistic workload: 63.4 us with, 60.0 us without).
   {
     const int nvec = P.metric == 1 ? NCACHE_VEC : NCACHE_VEC_DIAG;
     P.cache_stride = (nvec * P.ld + P.R * 3 + 1) & ~1;
     const size_t bytes = 4 * (size_t)P.cache_stride * sizeof(double);
-    P.cache = bytes <= 160 * 1024;
+    const bool rounds = use_rounds(m) && !p0 && !rc.flow;
+    P.cache = bytes <= 160 * 1024 && !rounds;
     if (P.cache) {
       GN_CUDA(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
       GN_CUDA(cudaFuncSetAttribute(k_advance, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));

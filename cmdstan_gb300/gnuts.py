@@ -112,7 +112,8 @@ class TrainArgs(ctypes.Structure):
 
 class LearnedArgs(ctypes.Structure):
     _fields_ = [("layers", ctypes.c_int), ("hidden", ctypes.c_int), ("clamp", ctypes.c_double),
-                ("train", TrainArgs), ("flow_warmup", ctypes.c_int), ("pilot_samples", ctypes.c_int),
+                ("train", TrainArgs), ("flow_warmup", ctypes.c_int), ("flow_delta", ctypes.c_double),
+                ("pilot_samples", ctypes.c_int),
                 ("moment_tolerance", ctypes.c_double)]
 
 

@@ -251,8 +251,8 @@ typedef struct {
   int steps, batch;         /* default 2000, 256 */
   double learning_rate;     /* default 2e-3 */
   double base_scale;        /* default 1.25 */
-  double beta0;             /* default 0.3 */
-  double anneal_fraction;   /* default 0.5 (0: no annealing) */
+  double beta0;             /* default 1 */
+  double anneal_fraction;   /* default 0 (no annealing) */
   unsigned int seed;
 } gnuts_train_args;
 void gnuts_train_args_default(gnuts_train_args* ta);
@@ -271,6 +271,7 @@ typedef struct {
   double clamp;             /* default 6 */
   gnuts_train_args train;   /* gnuts_train_args_default; the seed is derived from the sampler's */
   int flow_warmup;          /* z-space warmup iterations, default 300 */
+  double flow_delta;        /* adaptation target of the z-space sampler, default 0.95 */
   int pilot_samples;        /* draws per chain each sampler produces for the judge, default 200 */
   double moment_tolerance;  /* combined MCSE, default 4 */
 } gnuts_learned_args;
@@ -288,8 +289,8 @@ typedef struct {
 
 /* Learned-preconditioner variant of hmc_nuts_diag_e_adapt (command.hpp:
  * 673-688): (1) plain diag_e NUTS, num_warmup adaptive iterations and
- * pilot_samples draws; (2) flow initialised from those chains (mean of the
- * final positions, scale from the adapted inverse metric) and trained by
+ * pilot_samples draws; (2) flow initialised from those chains (median and
+ * MAD-based scale of their final positions, pooled across chains) and trained by
  * reverse KL through the model's own gradient kernels; (3) NUTS on z with
  * flow_warmup adaptive iterations and pilot_samples draws; (4) the judge
  * keeps the flow only if its ESS per gradient is not lower, its divergence

@@ -309,10 +309,33 @@ struct Config {
       sample->add(int_arg("num_chains", "Number of chains", 1, pos_i, " 0 < num_chains"));
       method->add(std::move(sample));
       // the other CmdStan methods are recognised (so that they parse like the
-      // reference's) and refused with a message when run
-      for (const char* m : {"optimize", "variational", "diagnose", "generate_quantities", "pathfinder",
-                            "log_prob", "laplace"})
-        method->add(group(m, "not provided by this sampler"));
+      // reference's); log_prob (arg_log_prob.hpp) and diagnose test=gradient
+      // (arg_diagnose.hpp, arg_test_gradient.hpp) run, the rest are refused
+      // with a message when run
+      for (const char* m : {"optimize", "variational"}) method->add(group(m, "not provided by this sampler"));
+      {
+        auto diag = group("diagnose", "Model diagnostics");
+        auto test = list("test", "Diagnostic test");
+        auto grad = group("gradient", "Check model gradient against finite differences");
+        grad->add(real_arg("epsilon", "Finite difference step size", 1e-6, pos_r, " 0 < epsilon"));
+        grad->add(real_arg("error", "Error threshold", 1e-6, pos_r, " 0 < error"));
+        test->add(std::move(grad));
+        diag->add(std::move(test));
+        method->add(std::move(diag));
+      }
+      for (const char* m : {"generate_quantities", "pathfinder"}) method->add(group(m, "not provided by this sampler"));
+      {
+        auto lp = group("log_prob", "Return the log density up to a constant and its gradients, given supplied "
+                                    "parameters");
+        lp->add(string_arg("unconstrained_params", "Input file (JSON or R dump) of parameter values on "
+                                                   "unconstrained scale", ""));
+        lp->add(string_arg("constrained_params", "Input file (JSON or R dump) of parameter values on "
+                                                 "constrained scale", ""));
+        lp->add(bool_arg("jacobian", "When true, include change-of-variables adjustment for constraining "
+                                     "parameter transforms", true));
+        method->add(std::move(lp));
+      }
+      method->add(group("laplace", "not provided by this sampler"));
     }
     id = int_arg("id", "Unique process identifier", 1, [](long long v) { return v >= 0; }, " id >= 0");
     data = group("data", "Input data options");

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <ctime>
+#include <random>
 #include <fstream>
 #include <iostream>
 #include <sstream>
@@ -151,6 +152,230 @@ std::vector<double> constrained_from_json(gnuts_model* m, const JValue& obj, int
   return out;
 }
 
+gnuts_model* create_model(const Config& cfg, const std::string& model_id) {
+  const std::string data_file = cfg.data->children[0]->sval;
+  const std::string data_text = data_file.empty() ? std::string("{}") : read_file(data_file);
+  gnuts_model* model = nullptr;
+  if (gnuts_model_create_json(model_id.c_str(), data_text.c_str(), cfg.random_seed, &model) != GNUTS_OK)
+    throw std::runtime_error("Error creating model '" + model_id + "': " + last_error());
+  return model;
+}
+
+void write_csv_header(std::ostream& f, gnuts_model* model, const std::vector<std::string>& cfg_lines) {
+  char nb[256];
+  gnuts_model_name(model, nb, sizeof nb);
+  f << "# stan_version_major = 2\n# stan_version_minor = 36\n# stan_version_patch = 0\n";
+  f << "# model = " << nb << "\n# start_datetime = " << utc_now() << "\n";
+  for (auto& l : cfg_lines) f << "# " << l << "\n";
+  f << "# stanc_version = gnuts built-in model\n# stancflags = \n# gnuts_version = " << gnuts_version() << "\n";
+}
+
+std::vector<std::string> split_csv(const std::string& line) {
+  std::vector<std::string> out;
+  std::stringstream ss(line);
+  std::string t;
+  while (std::getline(ss, t, ',')) {
+    while (!t.empty() && (t.back() == '\r' || t.back() == ' ')) t.pop_back();
+    while (!t.empty() && t.front() == ' ') t.erase(t.begin());
+    out.push_back(t);
+  }
+  return out;
+}
+
+// Unconstrained parameter sets for method=log_prob (command.hpp:414-446):
+// `unconstrained_params` is a JSON file with params_r (one vector, or an array
+// of vectors, command_helper.hpp:520-558); `constrained_params` is a JSON file
+// of the parameters block or a Stan CSV whose parameter columns are read row
+// by row (command_helper.hpp:279-374).
+std::vector<double> log_prob_points(gnuts_model* model, const std::string& upars, const std::string& cpars, int D,
+                                    int* n_out) {
+  std::vector<double> q;
+  if (!upars.empty()) {
+    JValue obj = JParser(read_file(upars)).parse();
+    const JValue* v = obj.get("params_r");
+    if (!v) throw std::runtime_error("Unconstrained parameters file has no variable 'params_r' with unconstrained "
+                                     "parameter values!");
+    std::vector<double> flat;
+    v->flatten(flat);
+    size_t cols = flat.size();
+    if (v->type == JValue::ARR && !v->arr.empty() && v->arr[0].type == JValue::ARR) cols = v->arr[0].arr.size();
+    if ((int)cols != D || flat.empty())
+      throw std::runtime_error("Incorrect number of unconstrained parameters provided! Model has " + std::to_string(D) +
+                               " parameters but " + std::to_string(cols) + " were found.");
+    *n_out = (int)(flat.size() / cols);
+    return flat;
+  }
+  std::vector<std::vector<double>> rows;
+  const size_t dot = cpars.find_last_of('.');
+  if (dot != std::string::npos && cpars.substr(dot) == ".csv") {
+    std::ifstream f(cpars);
+    if (!f) throw std::runtime_error("Can't open specified file, \"" + cpars + "\"");
+    std::string line;
+    std::vector<std::string> header;
+    std::vector<int> cols(D, -1);
+    while (std::getline(f, line)) {
+      if (line.empty() || line[0] == '#') continue;
+      if (header.empty()) {
+        header = split_csv(line);
+        for (int i = 0; i < D; ++i) {
+          char nb[256];
+          gnuts_model_param_name(model, i, 0, nb, sizeof nb);
+          for (size_t k = 0; k < header.size(); ++k)
+            if (header[k] == nb) cols[i] = (int)k;
+          if (cols[i] < 0)
+            throw std::runtime_error(std::string("Mismatch between model and fitted_parameters csv file \"") + cpars +
+                                     "\": no column " + nb);
+        }
+        continue;
+      }
+      const auto vals = split_csv(line);
+      std::vector<double> con(D);
+      for (int i = 0; i < D; ++i) {
+        if (cols[i] >= (int)vals.size()) throw std::runtime_error("short row in " + cpars);
+        con[i] = std::stod(vals[cols[i]]);
+      }
+      rows.push_back(con);
+    }
+  } else {
+    JValue obj = JParser(read_file(cpars)).parse();
+    rows.push_back(constrained_from_json(model, obj, D, cpars));
+  }
+  q.resize(rows.size() * D);
+  for (size_t r = 0; r < rows.size(); ++r)
+    if (gnuts_unconstrain(model, rows[r].data(), q.data() + r * D) != GNUTS_OK)
+      throw std::runtime_error("Error transforming the constrained parameter values of " + cpars + ": " +
+                               last_error());
+  *n_out = (int)rows.size();
+  return q;
+}
+
+// method=log_prob: lp and gradient for every parameter set, evaluated on the
+// GPU in one batch; written like services_log_prob_grad
+// (command_helper.hpp:560-600): header lp__,g_<unconstrained names>, one row
+// per set.
+int run_log_prob(Config& cfg, const std::string& model_id, Arg* lpg) {
+  const std::string upars = lpg->child("unconstrained_params")->sval;
+  const std::string cpars = lpg->child("constrained_params")->sval;
+  const bool jacobian = lpg->child("jacobian")->bval;
+  if (upars.empty() && cpars.empty())
+    throw std::runtime_error("No input parameter files provided, cannot calculate log probability density.");
+  if (!upars.empty() && !cpars.empty())
+    throw std::runtime_error("Cannot specify both input files of both constrained and unconstrained parameter "
+                             "values.");
+  const long long seed_arg = cfg.random->children[0]->ival;
+  cfg.random_seed = seed_arg >= 0 ? (unsigned)seed_arg : 0u;
+  const auto cfg_lines = cfg.lines();
+  for (auto& l : cfg_lines) std::cout << l << std::endl;
+  std::cout << std::endl;
+  gnuts_model* model = create_model(cfg, model_id);
+  struct ModelGuard { gnuts_model* m; ~ModelGuard() { gnuts_model_destroy(m); } } mg{model};
+  int D = 0, ncon = 0;
+  gnuts_model_dims(model, &D, &ncon);
+  int n = 0;
+  std::vector<double> q = log_prob_points(model, upars, cpars, D, &n);
+  std::vector<double> lp(n), g((size_t)n * D);
+  if (gnuts_log_prob_grad(model, n, q.data(), jacobian ? 1 : 0, lp.data(), g.data()) != GNUTS_OK)
+    throw std::runtime_error("Error during log_prob calculation:\n" + last_error());
+  Arg* out_grp = cfg.output.get();
+  const int sig_figs = (int)out_grp->child("sig_figs")->ival;
+  const int prec = sig_figs < 0 ? 6 : sig_figs;
+  const std::string file = out_grp->child("file")->sval;
+  std::ofstream f(file);
+  if (!f) throw std::runtime_error("Can't open output file " + file);
+  write_csv_header(f, model, cfg_lines);
+  f << "lp__";
+  for (int i = 0; i < D; ++i) {
+    char nb[256];
+    gnuts_model_param_name(model, i, 1, nb, sizeof nb);
+    f << ",g_" << nb;
+  }
+  f << "\n";
+  for (int r = 0; r < n; ++r) {
+    f << fmt(lp[r], prec);
+    for (int i = 0; i < D; ++i) f << "," << fmt(g[(size_t)r * D + i], prec);
+    f << "\n";
+  }
+  if (!f) throw std::runtime_error("error writing " + file);
+  return OK;
+}
+
+// method=diagnose test=gradient: the model gradient at the initial point
+// against central finite differences of the log density (with the Jacobian),
+// all 2D + 1 evaluations in one batch on the GPU.  Report as CmdStan's
+// gradient test prints it, to the console and as comments in the output file.
+int run_diagnose(Config& cfg, const std::string& model_id, Arg* diag) {
+  Arg* test = diag->child("test");
+  if (test->value_text() != "gradient") throw std::runtime_error("diagnose test=" + test->value_text() + " unknown");
+  Arg* grad = test->child("gradient");
+  const double eps = grad->child("epsilon")->rval, tol = grad->child("error")->rval;
+  const long long seed_arg = cfg.random->children[0]->ival;
+  cfg.random_seed = seed_arg >= 0
+                        ? (unsigned)seed_arg
+                        : (unsigned)(std::chrono::system_clock::now().time_since_epoch().count() & 0xFFFFFFFFu);
+  const auto cfg_lines = cfg.lines();
+  for (auto& l : cfg_lines) std::cout << l << std::endl;
+  std::cout << std::endl;
+  gnuts_model* model = create_model(cfg, model_id);
+  struct ModelGuard { gnuts_model* m; ~ModelGuard() { gnuts_model_destroy(m); } } mg{model};
+  int D = 0, ncon = 0;
+  gnuts_model_dims(model, &D, &ncon);
+  // initial point: a radius (uniform on (-R, R), seeded) or a JSON file of constrained values
+  std::vector<double> q0(D, 0.0);
+  const std::string init = cfg.init->sval;
+  double radius = 2.0;
+  bool is_radius = true;
+  try {
+    size_t used = 0;
+    radius = std::stod(init, &used);
+    is_radius = used == init.size();
+  } catch (...) {
+    is_radius = false;
+  }
+  if (is_radius) {
+    std::mt19937_64 rng(cfg.random_seed);
+    std::uniform_real_distribution<double> u(-radius, radius);
+    for (double& v : q0) v = radius > 0 ? u(rng) : 0.0;
+  } else {
+    JValue obj = JParser(read_file(init)).parse();
+    auto con = constrained_from_json(model, obj, D, init);
+    if (gnuts_unconstrain(model, con.data(), q0.data()) != GNUTS_OK)
+      throw std::runtime_error("Error transforming the initial values of " + init + ": " + last_error());
+  }
+  const int n = 2 * D + 1;
+  std::vector<double> q((size_t)n * D), lp(n), g((size_t)n * D);
+  for (int r = 0; r < n; ++r) std::copy(q0.begin(), q0.end(), q.begin() + (size_t)r * D);
+  for (int i = 0; i < D; ++i) {
+    q[(size_t)(1 + 2 * i) * D + i] += eps;
+    q[(size_t)(2 + 2 * i) * D + i] -= eps;
+  }
+  if (gnuts_log_prob_grad(model, n, q.data(), 1, lp.data(), g.data()) != GNUTS_OK)
+    throw std::runtime_error("Error during gradient test:\n" + last_error());
+  std::ostringstream rep;
+  rep << "TEST GRADIENT MODE\n\n Log probability=" << fmt(lp[0], 6) << "\n\n";
+  char line[256];
+  snprintf(line, sizeof line, " %10s %16s %16s %16s %16s\n", "param idx", "value", "model", "finite diff", "error");
+  rep << line;
+  int failed = 0;
+  for (int i = 0; i < D; ++i) {
+    const double fd = (lp[1 + 2 * i] - lp[2 + 2 * i]) / (2 * eps);
+    const double e = g[i] - fd;
+    if (std::fabs(e) > tol) ++failed;
+    snprintf(line, sizeof line, " %10d %16s %16s %16s %16s\n", i, fmt(q0[i], 6).c_str(), fmt(g[i], 6).c_str(),
+             fmt(fd, 6).c_str(), fmt(e, 6).c_str());
+    rep << line;
+  }
+  std::cout << rep.str() << std::endl;
+  const std::string file = cfg.output->child("file")->sval;
+  std::ofstream f(file);
+  if (!f) throw std::runtime_error("Can't open output file " + file);
+  write_csv_header(f, model, cfg_lines);
+  std::istringstream is(rep.str());
+  std::string l;
+  while (std::getline(is, l)) f << "# " << l << "\n";
+  if (failed) std::cout << failed << " of " << D << " gradient components differ by more than error=" << tol << std::endl;
+  return OK;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -190,6 +415,8 @@ int main(int argc, char** argv) {
   }
   try {
     const std::string method = cfg.method->value_text();
+    if (method == "log_prob") return run_log_prob(cfg, model_id, cfg.method->child("log_prob"));
+    if (method == "diagnose") return run_diagnose(cfg, model_id, cfg.method->child("diagnose"));
     if (method != "sample")
       throw std::runtime_error("method=" + method + " is not provided by gnuts-sample; it runs method=sample "
                                "(algorithm=hmc engine=nuts)");

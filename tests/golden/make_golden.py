@@ -2,7 +2,9 @@
 
 Reads the Stan CSV fixtures that the reference's stansummary / diagnose tests
 use (src/test/interface/example_output/*.csv under the reference checkout
-given as argv[1]) and writes, for each, a JSON file with the column names,
+given as argv[1]) and the fitted-parameters CSV of its log_prob tests
+(src/test/test-models/bern_fitted_params.csv), and writes, for each, a JSON
+file with the column names,
 the draw matrix and the comment blocks (config header, adaptation block,
 elapsed-time trailer).  The expected summary numbers are
 the literal goldens of src/test/interface/stansummary_test.cpp (:481-495,
@@ -42,11 +44,14 @@ def parse_stan_csv(path):
 
 def main(ref):
     here = os.path.dirname(os.path.abspath(__file__))
-    src = os.path.join(ref, "src", "test", "interface", "example_output")
-    for stem in ("bernoulli_chain_1", "eight_schools_output"):
-        names, rows, config, adapt, trailer = parse_stan_csv(os.path.join(src, stem + ".csv"))
+    fixtures = [("src/test/interface/example_output", "bernoulli_chain_1"),
+                ("src/test/interface/example_output", "eight_schools_output"),
+                # the fitted-parameters CSV of the log_prob method tests (log_prob_test.cpp:140-163)
+                ("src/test/test-models", "bern_fitted_params")]
+    for sub, stem in fixtures:
+        names, rows, config, adapt, trailer = parse_stan_csv(os.path.join(ref, sub, stem + ".csv"))
         out = {
-            "source": "src/test/interface/example_output/%s.csv" % stem,
+            "source": "%s/%s.csv" % (sub, stem),
             "names": names,
             "draws": rows,
             "config": config,

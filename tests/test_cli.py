@@ -251,3 +251,96 @@ def test_per_chain_init_files(tmp_path):
                       "file=" + data, "init=" + str(tmp_path / "bi.json"), "output", "refresh=0"], tmp_path)
     assert rc == 0, err
     assert os.path.exists(tmp_path / "output_1.csv") and os.path.exists(tmp_path / "output_2.csv")
+
+
+# ------------------------------------------------------------------ log_prob / diagnose
+def test_log_prob_needs_exactly_one_parameter_file(tmp_path):
+    """log_prob_test.cpp:165-174 (no parameters) and command.hpp:422-431 (both given)"""
+    data = write_json(tmp_path / "bern.data.json", BERN_DATA)
+    rc, _, err = run(["model=bernoulli", "method=log_prob", "data", "file=" + data], tmp_path)
+    assert rc == 1 and "No input parameter files provided" in err
+    up = write_json(tmp_path / "up.json", {"params_r": [0.1]})
+    rc, _, err = run(["model=bernoulli", "method=log_prob", "unconstrained_params=" + up,
+                      "constrained_params=" + up, "data", "file=" + data], tmp_path)
+    assert rc == 1 and "Cannot specify both" in err
+
+
+@pytest.mark.gpu
+def test_log_prob_constrained_csv_matches_oracle(tmp_path):
+    """log_prob_test.cpp:140-163: the bernoulli model on the reference's
+    fitted-parameters CSV (1000 draws, kept as tests/golden/bern_fitted_params.json)
+    gives 1000 rows of lp__, g_theta; every value equals the FP64 oracle's at
+    logit(theta) (the Jacobian included, as jacobian=true by default)."""
+    import numpy as np
+    import oracle
+    with open(os.path.join(ROOT, "tests", "golden", "bern_fitted_params.json")) as f:
+        g = json.load(f)
+    csv = tmp_path / "fitted.csv"
+    with open(csv, "w") as f:
+        f.write("# fitted parameters\n" + ",".join(g["names"]) + "\n")
+        for row in g["draws"]:
+            f.write(",".join(repr(v) for v in row) + "\n")
+    data = write_json(tmp_path / "bern.data.json", BERN_DATA)
+    rc, out, err = run(["model=bernoulli", "method=log_prob", "constrained_params=" + str(csv), "data",
+                        "file=" + data, "output", "file=lp.csv", "sig_figs=15"], tmp_path)
+    assert rc == 0, err
+    config, names, _, rows, _ = read_csv(tmp_path / "lp.csv")
+    assert names == ["lp__", "g_theta"]
+    assert len(rows) == 1000
+    om = oracle.OracleModel("bernoulli", BERN_DATA)
+    theta = np.array(g["draws"])[:, g["names"].index("theta")]
+    for th, (lp, gt) in zip(theta, rows):
+        olp, og = om.log_prob_grad([np.log(th / (1 - th))], jacobian=True)
+        assert abs(lp - olp) <= 1e-12 * abs(olp) + 1e-12 and abs(gt - og[0]) <= 1e-12 * max(1, abs(og[0]))
+    assert any("method = log_prob" in l for l in config)
+
+
+@pytest.mark.gpu
+def test_log_prob_unconstrained_json_and_jacobian(tmp_path):
+    """params_r as one vector or an array of vectors (command_helper.hpp:520-558);
+    jacobian=0 drops the change-of-variables term"""
+    import numpy as np
+    import oracle
+    from cmdstan_gb300 import workloads
+    d = workloads.eight_schools()
+    data = write_json(tmp_path / "es.json", {k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in d.items()})
+    rng = np.random.default_rng(2)
+    q = rng.uniform(-1, 1, (3, 10))
+    up = write_json(tmp_path / "up.json", {"params_r": q.tolist()})
+    om = oracle.OracleModel("hier", d)
+    for jac in (1, 0):
+        rc, _, err = run(["model=hier", "method=log_prob", "unconstrained_params=" + up, "jacobian=%d" % jac,
+                          "data", "file=" + data, "output", "file=lp%d.csv" % jac, "sig_figs=15"], tmp_path)
+        assert rc == 0, err
+        _, names, _, rows, _ = read_csv(tmp_path / ("lp%d.csv" % jac))
+        assert names[0] == "lp__" and len(names) == 11 and names[1] == "g_mu"
+        for qi, row in zip(q, rows):
+            olp, og = om.log_prob_grad(qi, jacobian=bool(jac))
+            assert abs(row[0] - olp) <= 1e-12 * abs(olp) + 1e-12
+            assert np.allclose(row[1:], og, rtol=1e-12, atol=1e-12)
+    bad = write_json(tmp_path / "short.json", {"params_r": [0.1, 0.2]})
+    rc, _, err = run(["model=hier", "method=log_prob", "unconstrained_params=" + bad, "data", "file=" + data],
+                     tmp_path)
+    assert rc == 1 and "Incorrect number of unconstrained parameters" in err
+
+
+@pytest.mark.gpu
+def test_diagnose_gradient_report(tmp_path):
+    """method=diagnose test=gradient (arg_test_gradient.hpp): the model
+    gradient against central finite differences at the initial point; every
+    error is within the default threshold for a correct model"""
+    from cmdstan_gb300 import workloads
+    d = workloads.eight_schools()
+    data = write_json(tmp_path / "es.json", {k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in d.items()})
+    rc, out, err = run(["model=hier", "method=diagnose", "test=gradient", "epsilon=1e-6", "error=1e-6", "data",
+                        "file=" + data, "random", "seed=7", "output", "file=diag.csv"], tmp_path)
+    assert rc == 0, err
+    assert "TEST GRADIENT MODE" in out and "Log probability=" in out
+    lines = [l for l in out.splitlines() if re.match(r"^\s+\d+\s", l)]
+    assert len(lines) == 10
+    for l in lines:
+        idx, value, model, fd, error = l.split()
+        assert abs(float(error)) < 1e-5, l
+        assert abs(float(model) - float(fd)) < 1e-5 * max(1.0, abs(float(model))), l
+    text = open(tmp_path / "diag.csv").read()
+    assert "# TEST GRADIENT MODE" in text and "method = diagnose" in text

@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "-I" + INC, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-I" + CSRC]
 
-CU_SOURCES = ["sampler.cu", "grad_tc.cu", "noalloc.cu", "flow.cu"]
+CU_SOURCES = ["sampler.cu", "grad_tc.cu", "noalloc.cu", "flow.cu", "summary_gpu.cu"]
 CPP_SOURCES = ["abi.cpp", "summary.cpp", "learned.cpp"]
 
 

@@ -36,6 +36,7 @@ EXPORTS = [
     "gnuts_flow_get_params", "gnuts_flow_init_affine", "gnuts_flow_forward", "gnuts_flow_inverse",
     "gnuts_flow_log_prob_grad", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
     "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt", "gnuts_train_args_default",
+    "gnuts_summary_columns_gpu",
 ]
 SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
 
@@ -59,17 +60,22 @@ def _summary_dict(out, probs):
     return r
 
 
-def summary_columns(draws, cols, probs=(0.05, 0.5, 0.95), threads=0):
-    """stansummary statistics of several columns of a [chains, draws, columns] array."""
+def summary_columns(draws, cols, probs=(0.05, 0.5, 0.95), threads=0, gpu=False):
+    """stansummary statistics of several columns of a [chains, draws, columns]
+    array; gpu=True computes them on the device (gnuts_summary_columns_gpu)."""
     lib = load()
     d = np.ascontiguousarray(draws, dtype=np.float64)
     C, n, K = d.shape
     cols = np.ascontiguousarray(cols, dtype=np.int32)
     p = np.ascontiguousarray(probs, dtype=np.float64)
     out = np.zeros((len(cols), 7 + len(p)))
-    _check(lib.gnuts_summary_columns(_dp(d), C, n, len(cols), n * K, K,
-                                     cols.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(p), len(p), threads,
-                                     _dp(out)))
+    ci = cols.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    if gpu:
+        rc = lib.gnuts_summary_columns_gpu(_dp(d), C, n, len(cols), n * K, K, ci, _dp(p), len(p), _dp(out))
+        if rc != GNUTS_OK:
+            raise GnutsError(rc, "device summary failed (code %d)" % rc)
+    else:
+        _check(lib.gnuts_summary_columns(_dp(d), C, n, len(cols), n * K, K, ci, _dp(p), len(p), threads, _dp(out)))
     return [_summary_dict(o, probs) for o in out]
 
 
@@ -176,6 +182,7 @@ def load():
     i64 = ctypes.c_int64
     lib.gnuts_summary.argtypes = [dp, ip, ip, i64, i64, dp, ip, dp]
     lib.gnuts_summary_columns.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, ip, dp]
+    lib.gnuts_summary_columns_gpu.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, dp]
     lib.gnuts_flow_create.argtypes = [ip, ip, ip, ctypes.c_double, ctypes.POINTER(vp)]
     lib.gnuts_flow_destroy.argtypes = [vp]
     lib.gnuts_flow_destroy.restype = None

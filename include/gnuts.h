@@ -176,6 +176,16 @@ int gnuts_summary_columns(const double* draws, int n_chains, int n_iter, int n_c
                           int64_t stride_iter, const int* cols, const double* probs, int n_probs,
                           int n_threads, double* out);
 
+/* The same statistics as gnuts_summary_columns (stansummary_helper.hpp:397-428),
+ * computed on the GPU, one CTA per quantity: the pooled draws are radix
+ * sorted on the device (draws, then their distances to the median) and every
+ * autocovariance is a CTA-wide reduction.  Results equal the host version's
+ * up to floating-point summation order.  n_iter >= 4 and n_chains * n_iter
+ * < 2^31.  Returns GNUTS_ERR_CUDA without a device. */
+int gnuts_summary_columns_gpu(const double* draws, int n_chains, int n_iter, int n_cols, int64_t stride_chain,
+                              int64_t stride_iter, const int* cols, const double* probs, int n_probs,
+                              double* out);
+
 /* Allocation-free gradient for callers that cannot allocate device memory.
  * No counterpart in the reference: CmdStan computes gradients on the host.
  * It exists for callers that run where cudaMalloc is not allowed -- code

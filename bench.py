@@ -300,14 +300,16 @@ def bench_horseshoe_gradient(chains=256):
                     "for K = 1000)"}
 
 
-def bench_funnel(chains=256):
-    """100-d funnel, 256 chains: plain diag_e NUTS vs the learned coupling map
-    (8 layers, hidden 128) with plain NUTS as judge; min bulk-ESS/s over all
-    parameters, each sampler timed end to end (warmup, training, judge
-    pilots and draws)."""
+def bench_learned(model_id, chains=256):
+    """Config 4, 256 chains: plain diag_e NUTS vs the learned coupling map
+    (8 layers, hidden 128) with plain NUTS as judge, on the centered
+    hierarchical model (J = 64) or the 100-d funnel; min bulk-ESS/s over all
+    parameters, each sampler timed end to end (warmup, training, judge pilots
+    and draws)."""
     import cmdstan_gb300 as gn
     from cmdstan_gb300 import workloads
-    m = gn.Model("funnel", workloads.funnel(100))
+    data = workloads.hier(seed=0) if model_id == "hier" else workloads.funnel(100)
+    m = gn.Model(model_id, data)
     t0 = time.perf_counter()
     fp = m.sample(num_chains=chains, num_warmup=NUM_WARMUP, num_samples=NUM_SAMPLES, seed=21, refresh=0)
     tp = time.perf_counter() - t0
@@ -317,8 +319,11 @@ def bench_funnel(chains=256):
                                refresh=0)
     tl = time.perf_counter() - t0
     el, rl = _min_ess_rhat(fl.draws)
-    return {"cpu_baseline": _oracle_rate("funnel", workloads.funnel(100), 16, 5.0),
-            "workload": "funnel v ~ N(0,3), x_1..100 ~ N(0, exp(v/2)); %d chains; 1000 warmup + 1000 draws" % chains,
+    desc = ("centered hierarchical J=64: mu ~ N(0,5), tau ~ half-Cauchy(0,5), theta_j ~ N(mu,tau), "
+            "y_j ~ N(theta_j, sigma_j), sigma_j ~ U[5,20], y at mu=4, tau=3" if model_id == "hier" else
+            "funnel v ~ N(0,3), x_1..100 ~ N(0, exp(v/2))")
+    return {"cpu_baseline": _oracle_rate(model_id, data, 16, 5.0),
+            "workload": "%s; %d chains; 1000 warmup + 1000 draws" % (desc, chains),
             "plain": {"min_bulk_ess_per_s": ep / tp, "min_bulk_ess": ep, "rhat_max": rp, "seconds": tp,
                       "divergence_rate": float(fp.draws[:, :, 5].mean()),
                       "grad_evals": float(fp.n_leapfrog.sum())},
@@ -408,7 +413,14 @@ def main():
     # ESS / R-hat of the last run
     last = fits[-1]
     cols = list(range(7, last.draws.shape[2]))
-    sm = gnuts.summary_columns(last.draws, cols, threads=os.cpu_count() or 8)
+    t_sum = time.perf_counter()
+    try:
+        sm = gnuts.summary_columns(last.draws, cols, gpu=True)
+        summary_where = "gpu"
+    except Exception:
+        sm = gnuts.summary_columns(last.draws, cols, threads=os.cpu_count() or 8)
+        summary_where = "host"
+    t_sum = time.perf_counter() - t_sum
     ess_min = float(min(s["ess_bulk"] for s in sm))
     rhat_max = float(max(s["rhat"] for s in sm))
     step_s = last.timing["device_ms"] / 1e3
@@ -450,12 +462,16 @@ def main():
         "e2e": {"value": e2e_value, "unit": "grad-evals/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": float(np.mean(e2e_times))},
         "gpu_launches": launches, "clocks": clocks,
+        "summary": {"where": summary_where, "seconds": t_sum,
+                    "what": "stansummary statistics of the 101 parameters over 1024 x 1000 draws"},
     }
     if rank == 0:
         if not args.no_extra:
             extra = {}
             for name, fn in (("bernoulli", bench_bernoulli), ("varint_set_512x4", lambda: bench_varint_set(peaks)),
-                             ("funnel_100d", bench_funnel), ("horseshoe_gradient", bench_horseshoe_gradient)):
+                             ("hier_64_learned_vs_plain", lambda: bench_learned("hier")),
+                             ("funnel_100d_learned_vs_plain", lambda: bench_learned("funnel")),
+                             ("horseshoe_gradient", bench_horseshoe_gradient)):
                 try:
                     extra[name] = fn()
                 except Exception as e:  # reported in the line, the headline stands

@@ -149,46 +149,65 @@ static __device__ __noinline__ double lpg_logistic(const DevModel& M, const doub
 // ---- varint: [alpha_1..J, beta_1..K, log sigma_y, log tau]; rows sorted by group.
 // Members of a posterior set order the parameters [beta, log sigma_y, log tau,
 // alpha] (alpha_last) and may evaluate the rows in FP32 (fp32): each lane sums
-// its rows of one group in FP32 and adds the group's partial sums to FP64
-// accumulators, so the FP32 rounding never spans more than one group.
+// its rows in FP32 over blocks of VG groups and adds each block's partial
+// sums to FP64 accumulators, so the FP32 rounding never spans more than VG
+// groups.  The per-group scalar terms (alpha prior, its gradient) are spread
+// over the lanes instead of being repeated by every lane.
+constexpr int VG = 8;
 template <class T>
-__device__ __forceinline__ void varint_rows(const DevModel& M, int r0, int r1, double a, const double* bb, double isy,
-                                            double& ss, double& gr, double* gb, int lane) {
-  const int K = M.K;
+__device__ __forceinline__ double varint_likelihood(const DevModel& M, const double* al, const double* bb,
+                                                    double isy, double* g_al, double* gb, int lane) {
+  const int J = M.J, K = M.K;
   T b[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) b[k] = (T)(k < K ? bb[k] : 0.0);
-  const T ta = (T)a, tisy = (T)isy;
-  T s2 = 0, g1 = 0, gk[16];
+  const T tisy = (T)isy;
+  double ss = 0;
+  T s2 = 0, gk[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) gk[k] = 0;
-  for (int n = r0 + lane; n < r1; n += 32) {
-    T x[16];
-    if constexpr (sizeof(T) == 4) {
-      const float* xr = M.Xf + (size_t)n * K;
+  for (int j = 0; j < J; ++j) {
+    const T ta = (T)al[j];
+    T g1 = 0;
+    const int r0 = M.gstart[j], r1 = M.gstart[j + 1];
+    for (int n = r0 + lane; n < r1; n += 32) {
+      T x[16];
+      if constexpr (sizeof(T) == 4) {
+        const float* xr = M.Xf + (size_t)n * K;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.f;
-    } else {
-      const double* xr = M.X + (size_t)n * K;
+        for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.f;
+      } else {
+        const double* xr = M.X + (size_t)n * K;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.0;
+        for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.0;
+      }
+      T mu = ta;
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (k < K) mu += x[k] * b[k];
+      const T e = ((T)M.yr[n] - mu) * tisy;
+      s2 += e * e;
+      const T r = e * tisy;
+      g1 += r;
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (k < K) gk[k] += r * x[k];
     }
-    T mu = ta;
+    // group sum of the residuals (same order on every lane)
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
-      if (k < K) mu += x[k] * b[k];
-    const T e = ((T)M.yr[n] - mu) * tisy;
-    s2 += e * e;
-    const T r = e * tisy;
-    g1 += r;
+    for (int o = 16; o > 0; o >>= 1) g1 += __shfl_xor_sync(GN_FULL, g1, o);
+    if (lane == (j & 31)) g_al[j] = (double)g1;
+    if ((j % VG) == VG - 1 || j == J - 1) {
+      ss += (double)s2;
+      s2 = 0;
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
-      if (k < K) gk[k] += r * x[k];
+      for (int k = 0; k < 16; ++k) {
+        gb[k] += (double)gk[k];
+        gk[k] = 0;
+      }
+    }
   }
-  ss += (double)s2;
-  gr = (double)g1;
-#pragma unroll
-  for (int k = 0; k < 16; ++k) gb[k] += (double)gk[k];
+  return ss;
 }
 
 static __device__ __noinline__ double lpg_varint(const DevModel& M, const double* q, double* g, int jac, int lane) {
@@ -197,26 +216,27 @@ static __device__ __noinline__ double lpg_varint(const DevModel& M, const double
   const double* al = q + ia;
   const double* be = q + ib;
   double ls = q[is], lt = q[is + 1];
-  double sy = exp(ls), tau = exp(lt), isy = 1.0 / sy;
+  double sy = exp(ls), tau = exp(lt), isy = 1.0 / sy, itau = 1.0 / tau;
   double bb[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) bb[k] = k < K ? be[k] : 0.0;
   double gb[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) gb[k] = 0.0;
-  double ss = 0, lpa = 0, glt = 0;
-  for (int j = 0; j < J; ++j) {
-    double a = al[j];
-    double gr = 0;
-    int r0 = M.gstart[j], r1 = M.gstart[j + 1];
-    if (M.fp32) varint_rows<float>(M, r0, r1, a, bb, isy, ss, gr, gb, lane);
-    else varint_rows<double>(M, r0, r1, a, bb, isy, ss, gr, gb, lane);
-    gr = wsum(gr);
-    double z = a / tau;
-    if (lane == 0) g[ia + j] = gr - z / tau;
+  // likelihood: residual sums per group into g[ia + j], shared coefficients into gb
+  double ss = M.fp32 ? varint_likelihood<float>(M, al, bb, isy, g + ia, gb, lane)
+                     : varint_likelihood<double>(M, al, bb, isy, g + ia, gb, lane);
+  __syncwarp();
+  // alpha_j ~ normal(0, tau), lane-parallel over groups
+  double lpa = 0, glt = 0;
+  for (int j = lane; j < J; j += 32) {
+    const double z = al[j] * itau;
+    g[ia + j] -= z * itau;
     lpa += -lt - 0.5 * z * z;
     glt += -1.0 + z * z;
   }
+  lpa = wsum(lpa);
+  glt = wsum(glt);
   ss = wsum(ss);
   double pb = 0;
 #pragma unroll

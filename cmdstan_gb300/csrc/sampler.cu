@@ -457,6 +457,7 @@ int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, d
 
 struct RunStats {
   double rounds = 0, grad_us = 0, advance_us = 0, device_ms = 0, launches = 0, reduce_us = 0;
+  double chains_per_cta = 4;
 };
 
 static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double per_chain_max, int refresh,
@@ -740,8 +741,50 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     GN_CUDA(cudaEventCreate(&f1));
     struct FEv { cudaEvent_t a, b; ~FEv() { cudaEventDestroy(a); cudaEventDestroy(b); } } fev{f0, f1};
     GN_CUDA(cudaEventRecord(f0));
-    for (long long l = 0; l < max_launches; ++l) {
-      k_fused<<<blocks, threads, cache_bytes(P)>>>(P, B, m.dev, RB);
+    // Launch shape autotuner: chains per CTA (1, 2 or 4 warps) and whether the
+    // chain vectors are cached in shared memory.  Each candidate runs one
+    // short launch of the real run (the chains advance; what a chain computes
+    // does not depend on the launch shape), and the fastest one is kept.
+    int warps = 4;
+    if (C >= 64 && !p0) {
+      cudaEvent_t t0, t1;
+      GN_CUDA(cudaEventCreate(&t0));
+      GN_CUDA(cudaEventCreate(&t1));
+      struct TEv { cudaEvent_t a, b; ~TEv() { cudaEventDestroy(a); cudaEventDestroy(b); } } tev{t0, t1};
+      const int cache_ok = P.cache;
+      Params Pt = P;
+      Pt.grad_budget = 32;
+      float best = 1e30f;
+      int best_w = 4, best_c = cache_ok;
+      for (int w : {4, 2, 1})
+        for (int cch = cache_ok; cch >= 0; --cch) {
+          Pt.cache = cch;
+          const int bl = (C + w - 1) / w;
+          const size_t sm = cch ? (size_t)w * P.cache_stride * sizeof(double) : 0;
+          GN_CUDA(cudaEventRecord(t0));
+          k_fused<<<bl, 32 * w, sm>>>(Pt, B, m.dev, RB);
+          GN_CUDA(cudaGetLastError());
+          GN_CUDA(cudaEventRecord(t1));
+          GN_CUDA(cudaEventSynchronize(t1));
+          float ms = 0;
+          cudaEventElapsedTime(&ms, t0, t1);
+          stats.rounds += 1;
+          stats.launches += 1;
+          if (ms < best) {
+            best = ms;
+            best_w = w;
+            best_c = cch;
+          }
+        }
+      warps = best_w;
+      P.cache = best_c;
+      stats.chains_per_cta = warps;
+      GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    const int fthreads = 32 * warps, fblocks = (C + warps - 1) / warps;
+    const size_t fsmem = P.cache ? (size_t)warps * P.cache_stride * sizeof(double) : 0;
+    for (long long l = 0; l < max_launches && done < C; ++l) {
+      k_fused<<<fblocks, fthreads, fsmem>>>(P, B, m.dev, RB);
       GN_CUDA(cudaGetLastError());
       stats.rounds += 1;
       stats.launches += 1;
@@ -794,6 +837,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       out->timing[GNUTS_TIMING_DEVICE_MS] = stats.device_ms;
       out->timing[GNUTS_TIMING_LAUNCHES] = stats.launches;
       out->timing[GNUTS_TIMING_REDUCE_US] = stats.reduce_us;
+      out->timing[GNUTS_TIMING_CHAINS_PER_CTA] = stats.chains_per_cta;
     }
   }
   if (counters)

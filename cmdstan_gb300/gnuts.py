@@ -136,7 +136,8 @@ class LearnedReport(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "launches", "reduce_kernel_us"]
+TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "launches", "reduce_kernel_us",
+                 "chains_per_cta"]
 
 
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int)

@@ -124,6 +124,7 @@ typedef struct {
 #define GNUTS_TIMING_DEVICE_MS 3     /* device time from first to last launch, ms */
 #define GNUTS_TIMING_LAUNCHES 4      /* kernels launched by the run */
 #define GNUTS_TIMING_REDUCE_US 5     /* 0: the row-split sums run inside the state-machine kernel */
+#define GNUTS_TIMING_CHAINS_PER_CTA 6  /* launch shape the fused-mode autotuner picked (chains per CTA) */
 #define GNUTS_TIMING_FIELDS 8
 
 /* Progress callback, called from the calling thread between device launches

@@ -148,56 +148,78 @@ static __device__ __noinline__ double lpg_logistic(const DevModel& M, const doub
 
 // ---- varint: [alpha_1..J, beta_1..K, log sigma_y, log tau]; rows sorted by group.
 // Members of a posterior set order the parameters [beta, log sigma_y, log tau,
-// alpha] (alpha_last) and may evaluate the rows in FP32 (fp32): each lane sums
-// its rows in FP32 over blocks of VG groups and adds each block's partial
-// sums to FP64 accumulators, so the FP32 rounding never spans more than VG
-// groups.  The per-group scalar terms (alpha prior, its gradient) are spread
-// over the lanes instead of being repeated by every lane.
-constexpr int VG = 8;
+// alpha] (alpha_last) and may evaluate the rows in FP32 (fp32).  The
+// per-group scalar terms (alpha prior, its gradient) are spread over the
+// lanes instead of being repeated by every lane.
+// Rows are streamed independently of group boundaries: each lane takes rows
+// lane, lane + 32, ..., four at a time with all their loads issued together;
+// the residual sums per group (rows are sorted by group, so a warp's 32 rows
+// span a few groups) are segmented warp reductions whose segment-end lane
+// adds its total into g_al.  Row sums of squares and coefficient gradients
+// are FP32 (T) per lane, added to FP64 every VR rows.
+constexpr int VU = 4;   // rows per lane in flight
+constexpr int VR = 32;  // rows per lane between FP64 flushes
 template <class T>
 __device__ __forceinline__ double varint_likelihood(const DevModel& M, const double* al, const double* bb,
                                                     double isy, double* g_al, double* gb, int lane) {
-  const int J = M.J, K = M.K;
+  const int J = M.J, K = M.K, N = M.N;
   T b[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) b[k] = (T)(k < K ? bb[k] : 0.0);
   const T tisy = (T)isy;
+  for (int j = lane; j < J; j += 32) g_al[j] = 0.0;
+  __syncwarp();
   double ss = 0;
   T s2 = 0, gk[16];
 #pragma unroll
   for (int k = 0; k < 16; ++k) gk[k] = 0;
-  for (int j = 0; j < J; ++j) {
-    const T ta = (T)al[j];
-    T g1 = 0;
-    const int r0 = M.gstart[j], r1 = M.gstart[j + 1];
-    for (int n = r0 + lane; n < r1; n += 32) {
-      T x[16];
+  int since = 0;
+  for (int base = 0; base < N; base += 32 * VU) {
+    T x[VU][16], yv[VU];
+    int grp[VU];
+#pragma unroll
+    for (int u = 0; u < VU; ++u) {
+      const int n = base + 32 * u + lane;
+      const bool ok = n < N;
+      grp[u] = ok ? M.group[n] - 1 : 0x7fffffff;
+      yv[u] = ok ? (T)M.yr[n] : (T)0;
       if constexpr (sizeof(T) == 4) {
-        const float* xr = M.Xf + (size_t)n * K;
+        const float* xr = M.Xf + (size_t)(ok ? n : 0) * K;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.f;
+        for (int k = 0; k < 16; ++k) x[u][k] = (ok && k < K) ? xr[k] : 0.f;
       } else {
-        const double* xr = M.X + (size_t)n * K;
+        const double* xr = M.X + (size_t)(ok ? n : 0) * K;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) x[k] = k < K ? xr[k] : 0.0;
+        for (int k = 0; k < 16; ++k) x[u][k] = (ok && k < K) ? xr[k] : 0.0;
       }
-      T mu = ta;
-#pragma unroll
-      for (int k = 0; k < 16; ++k)
-        if (k < K) mu += x[k] * b[k];
-      const T e = ((T)M.yr[n] - mu) * tisy;
-      s2 += e * e;
-      const T r = e * tisy;
-      g1 += r;
-#pragma unroll
-      for (int k = 0; k < 16; ++k)
-        if (k < K) gk[k] += r * x[k];
     }
-    // group sum of the residuals (same order on every lane)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) g1 += __shfl_xor_sync(GN_FULL, g1, o);
-    if (lane == (j & 31)) g_al[j] = (double)g1;
-    if ((j % VG) == VG - 1 || j == J - 1) {
+    for (int u = 0; u < VU; ++u) {
+      const bool ok = grp[u] != 0x7fffffff;
+      T mu = ok ? (T)al[grp[u]] : (T)0;
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (k < K) mu += x[u][k] * b[k];
+      const T e = ok ? (yv[u] - mu) * tisy : (T)0;
+      s2 += e * e;
+      T r = e * tisy;
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (k < K) gk[k] += r * x[u][k];
+      // segmented inclusive sum of r over lanes with the same group (keys ascend with the lane)
+      const int key = grp[u];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const T rv = __shfl_up_sync(GN_FULL, r, o);
+        const int kv = __shfl_up_sync(GN_FULL, key, o);
+        if (lane >= o && kv == key) r += rv;
+      }
+      const int next = __shfl_down_sync(GN_FULL, key, 1);
+      if (ok && (lane == 31 || next != key)) g_al[key] += (double)r;
+      __syncwarp();
+    }
+    since += VU;
+    if (since >= VR || base + 32 * VU >= N) {
       ss += (double)s2;
       s2 = 0;
 #pragma unroll
@@ -205,6 +227,7 @@ __device__ __forceinline__ double varint_likelihood(const DevModel& M, const dou
         gb[k] += (double)gk[k];
         gk[k] = 0;
       }
+      since = 0;
     }
   }
   return ss;

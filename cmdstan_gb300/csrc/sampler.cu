@@ -331,6 +331,7 @@ int upload(Model& m, std::string& err) {
       e.Xf = d.Xf + (size_t)s.row_off * d.K;
       e.Xb = d.Xb + (size_t)s.row_off * d.K;
       e.yr = d.yr + s.row_off;
+      e.group = d.group + s.row_off;
       e.gstart = d.gstart + s.g_off;
       e.members = nullptr;
       e.n_members = 0;

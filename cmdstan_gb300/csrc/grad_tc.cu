@@ -451,7 +451,8 @@ EncodeTiled get_encode(std::string& err) {
   if (fn) return fn;
   void* p = nullptr;
   cudaDriverEntryPointQueryResult q;
-  cudaError_t e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q);
+  // the entry point as introduced (CUDA 12.0)
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
   if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
     err = "cuTensorMapEncodeTiled unavailable";
     return nullptr;

@@ -640,6 +640,12 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     if (P.cache) {
       GN_CUDA(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
       GN_CUDA(cudaFuncSetAttribute(k_advance, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    } else if (!rounds && (size_t)P.cache_stride * sizeof(double) <= 200 * 1024) {
+      // large chains: the cache can still hold one or two chains per CTA
+      // (the fused-mode autotuner decides whether that pays)
+      const size_t one = (size_t)P.cache_stride * sizeof(double);
+      GN_CUDA(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)std::min<size_t>(2 * one <= 200 * 1024 ? 2 * one : one, 200 * 1024)));
     }
   }
 
@@ -752,13 +758,14 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       GN_CUDA(cudaEventCreate(&t0));
       GN_CUDA(cudaEventCreate(&t1));
       struct TEv { cudaEvent_t a, b; ~TEv() { cudaEventDestroy(a); cudaEventDestroy(b); } } tev{t0, t1};
-      const int cache_ok = P.cache;
       Params Pt = P;
       Pt.grad_budget = 32;
       float best = 1e30f;
-      int best_w = 4, best_c = cache_ok;
+      int best_w = 4, best_c = P.cache;
       for (int w : {4, 2, 1})
-        for (int cch = cache_ok; cch >= 0; --cch) {
+        for (int cch = 1; cch >= 0; --cch) {
+          // shared-memory budget of a CTA's cached chains (as set above)
+          if (cch && (size_t)w * P.cache_stride * sizeof(double) > (w == 4 ? 160 : 200) * 1024) continue;
           Pt.cache = cch;
           const int bl = (C + w - 1) / w;
           const size_t sm = cch ? (size_t)w * P.cache_stride * sizeof(double) : 0;

@@ -251,7 +251,7 @@ inline void print_arg(const Arg& a, int depth, std::vector<std::string>& out) {
 
 // ---------------------------------------------------------------- the tree
 struct Config {
-  std::unique_ptr<Arg> method, id, data, init, random, output, num_threads;
+  std::unique_ptr<Arg> method, id, data, init, random, output, num_threads, gpu;
   std::vector<Arg*> top;        // print / parse order
   unsigned int random_seed = 0; // value used when seed is left at -1
 
@@ -360,7 +360,18 @@ struct Config {
     output->add(bool_arg("save_cmdstan_config", "Save the CmdStan configuration as JSON?", false));
     num_threads = int_arg("num_threads", "Number of threads available to the program.", 1,
                           [](long long v) { return v > 0 || v == -1; }, " num_threads > 0 || num_threads == -1");
-    top = {method.get(), id.get(), data.get(), init.get(), random.get(), output.get(), num_threads.get()};
+    // options of this sampler that CmdStan does not have, in their own group so
+    // that CmdStan's arguments and defaults stay as they are
+    gpu = group("gpu", "GB300 sampler options (not part of CmdStan)");
+    {
+      auto prec = list("precision", "Gradient precision of the data-heavy models");
+      prec->add(unvalued("fp64", "FP64 everywhere"));
+      prec->add(unvalued("mixed", "BF16-split tensor-core contractions, FP32 accumulation, FP64 energy"));
+      gpu->add(std::move(prec));
+      gpu->add(bool_arg("learned", "Learned affine-coupling preconditioner with plain NUTS as fallback and judge "
+                                   "(metric=diag_e, adaptation engaged)", false));
+    }
+    top = {method.get(), id.get(), data.get(), init.get(), random.get(), output.get(), num_threads.get(), gpu.get()};
   }
 
   Arg* sample() const { return method->children[0].get(); }

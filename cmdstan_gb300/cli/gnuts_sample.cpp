@@ -545,7 +545,11 @@ int main(int argc, char** argv) {
     a.init_buffer = (unsigned)adapt->child("init_buffer")->ival;
     a.term_buffer = (unsigned)adapt->child("term_buffer")->ival;
     a.window = (unsigned)adapt->child("window")->ival;
+    a.precision = cfg.gpu->child("precision")->value_text() == "mixed" ? GNUTS_PRECISION_MIXED : GNUTS_PRECISION_FP64;
     if (const char* p = std::getenv("GNUTS_PRECISION")) a.precision = std::string(p) == "mixed" ? 1 : 0;
+    const bool learned = cfg.gpu->child("learned")->bval;
+    if (learned && (metric != "diag_e" || !engaged))
+      throw std::runtime_error("gpu learned=1 needs metric=diag_e with adaptation engaged");
 
     const int n_saved = (save_warmup ? (num_warmup + thin - 1) / thin : 0) + (num_samples + thin - 1) / thin;
     const int ncol = 7 + ncon;
@@ -568,7 +572,18 @@ int main(int argc, char** argv) {
     const double* mp = inv_metric.empty() ? nullptr : inv_metric.data();
     int rc;
     gnuts_progress_fn pf = refresh > 0 ? on_progress : nullptr;
-    if (engaged) {
+    if (learned) {
+      // warmup and judge pilots run inside; out receives the kept sampler's draws
+      gnuts_learned_args la;
+      gnuts_learned_args_default(&la);
+      gnuts_learned_report rep;
+      rc = gnuts_hmc_nuts_learned_diag_e_adapt(model, &a, &la, ip, &out, &rep, pf, &prog);
+      if (rc == GNUTS_OK)
+        std::cout << "Learned preconditioner: " << (rep.used_flow ? "kept" : "rejected, plain NUTS kept")
+                  << " (pilot ESS per gradient " << fmt(rep.flow_ess_per_grad, 3) << " vs "
+                  << fmt(rep.plain_ess_per_grad, 3) << ", divergences " << fmt(rep.flow_divergence_rate, 3)
+                  << " vs " << fmt(rep.plain_divergence_rate, 3) << ")" << std::endl;
+    } else if (engaged) {
       if (metric == "dense_e") rc = gnuts_hmc_nuts_dense_e_adapt(model, &a, ip, mp, &out, pf, &prog);
       else if (metric == "diag_e") rc = gnuts_hmc_nuts_diag_e_adapt(model, &a, ip, mp, &out, pf, &prog);
       else rc = gnuts_hmc_nuts_unit_e_adapt(model, &a, ip, &out, pf, &prog);

@@ -912,6 +912,7 @@ int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, dou
 }
 
 int flow_train(Model& m, Flow& f, const gnuts_train_args& ta, double* loss_trace, std::string& err) {
+  NvtxRange range("gnuts.flow.train");
   const int steps = ta.steps, batch = ta.batch;
   const double lr = ta.learning_rate;
   int rc = upload(m, err);

@@ -4,9 +4,19 @@
 #include <stdint.h>
 #include <string>
 #include <vector>
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/gnuts.h"
 
 namespace gnuts {
+
+// NVTX range for the duration of a scope (visible in Nsight timelines; a no-op
+// when no tool is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 enum ModelKind : int {
   MK_BERNOULLI = 0,

@@ -257,6 +257,7 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   if (rc) return api_fail(rc, err);
   std::unique_ptr<Flow> flow_owner(fl);
 
+  NvtxRange range("gnuts.learned");
   // (1) plain diag_e NUTS: adaptive warmup and a pilot
   double t0 = now_s();
   gnuts_sample_args ap = *a;
@@ -342,6 +343,7 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
     for (int c = 0; c < C; ++c) rep.flow_grads += rf.nlf[c];
 
   // (4) judge
+  NvtxRange judge_range("gnuts.learned.judge");
   const PilotStats sp = pilot_stats(rp.draws, C, P, ncol);
   rep.plain_ess_per_grad = sp.min_ess / std::max(1.0, sp.grads);
   rep.plain_divergence_rate = sp.div_rate;

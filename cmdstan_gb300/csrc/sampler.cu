@@ -588,6 +588,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                          const double* inv_metric, const double* p0, const unsigned* chain_ids,
                          uint64_t* counters, double* replay_q_out, gnuts_output* out,
                          gnuts_progress_fn progress, void* ctx, std::string& err) {
+  NvtxRange range(rc.flow ? "gnuts.nuts.flow" : (rc.adapt ? "gnuts.nuts.adapt" : "gnuts.nuts"));
   int st = upload(m, err);
   if (st) return st;
   if ((st = check_warp_limits(m, err))) return st;
@@ -822,6 +823,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     return GNUTS_ERR_TIMEOUT;
   }
 
+  NvtxRange out_range("gnuts.nuts.copy_out");
   std::vector<Scal> sc(C);
   GN_CUDA(cudaMemcpy(sc.data(), B.sc, sizeof(Scal) * C, cudaMemcpyDeviceToHost));
   if (out) {

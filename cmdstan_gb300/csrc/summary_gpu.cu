@@ -12,6 +12,7 @@
 // MAD from those two orders; the autocovariances behind every ESS are
 // CTA-wide reductions, eight lags per pass over the draws.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -517,6 +518,8 @@ extern "C" int gnuts_summary_columns_gpu(const double* draws, int n_chains, int 
     return GNUTS_ERR_ARGUMENT;
   if ((long long)n_chains * n_iter >= (1ll << 31)) return GNUTS_ERR_ARGUMENT;
   if (n_cols == 0) return GNUTS_OK;
+  nvtxRangePushA("gnuts.summary.gpu");
+  struct Pop { ~Pop() { nvtxRangePop(); } } pop;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GNUTS_ERR_CUDA;
   const int M = n_chains, n = n_iter;

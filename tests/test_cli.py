@@ -344,3 +344,33 @@ def test_diagnose_gradient_report(tmp_path):
         assert abs(float(model) - float(fd)) < 1e-5 * max(1.0, abs(float(model))), l
     text = open(tmp_path / "diag.csv").read()
     assert "# TEST GRADIENT MODE" in text and "method = diagnose" in text
+
+
+# ------------------------------------------------------------------ gpu options
+def test_gpu_group_echo_and_learned_needs_diag_adapt(tmp_path):
+    """The sampler's own options sit in a `gpu` group after CmdStan's
+    arguments; learned=1 is refused outside diag_e with adaptation."""
+    _, out, _ = run(["model=bernoulli", "sample", "num_warmup=0", "adapt", "engaged=1"], tmp_path)
+    keys = key_lines([l for l in out.splitlines() if l.strip()])
+    assert keys[-3:] == ["gpu", "  precision", "  learned"]
+    data = write_json(tmp_path / "bern.data.json", BERN_DATA)
+    rc, _, err = run(["model=bernoulli", "sample", "algorithm=hmc", "metric=dense_e", "data", "file=" + data,
+                      "gpu", "learned=1"], tmp_path)
+    assert rc == 1 and "learned=1 needs metric=diag_e" in err
+
+
+@pytest.mark.gpu
+def test_gpu_learned_run_writes_stan_csv(tmp_path):
+    from cmdstan_gb300 import workloads
+    d = workloads.eight_schools()
+    data = write_json(tmp_path / "es.json", {k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in d.items()})
+    rc, out, err = run(["model=hier", "sample", "num_samples=100", "num_warmup=200", "num_chains=32", "data",
+                        "file=" + data, "random", "seed=3", "output", "file=lr.csv", "refresh=0", "gpu",
+                        "learned=1"], tmp_path)
+    assert rc == 0, err
+    assert "Learned preconditioner:" in out
+    config, names, adapt, rows, _ = read_csv(tmp_path / "lr_1.csv")
+    assert names[:7] == ["lp__", "accept_stat__", "stepsize__", "treedepth__", "n_leapfrog__", "divergent__",
+                         "energy__"] and names[7] == "mu"
+    assert len(rows) == 100
+    assert any(l.startswith("#   learned = true") or l.startswith("# ") and "learned = true" in l for l in config)

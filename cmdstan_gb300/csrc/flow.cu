@@ -238,12 +238,13 @@ __device__ __forceinline__ void adj_layer(const FlowDev& F, int l, const __nv_bf
     pk[k] = hb[k] * (1.0f - h * h);
     pb[j0 + k] = pk[k];
   }
-  // u_b adjoint += W1 pbar: 32 rows per pass, then a reduce-scatter leaves the
-  // sum of row r0 + L on lane L (31 shuffles per 32 rows)
-  for (int r0 = 0; r0 < nb; r0 += 32) {
-    float part[32];
+  // u_b adjoint += W1 pbar: 16 rows per pass; the two half-warps' partials
+  // are folded, then a reduce-scatter over 16 lanes leaves the sum of row
+  // r0 + (L mod 16) on lane L (31 shuffles per 16 rows, 16 registers)
+  for (int r0 = 0; r0 < nb; r0 += 16) {
+    float part[16];
 #pragma unroll
-    for (int q = 0; q < 32; ++q) {
+    for (int q = 0; q < 16; ++q) {
       float t = 0.f;
       if (r0 + q < nb) {
         float w[HPL];
@@ -254,7 +255,9 @@ __device__ __forceinline__ void adj_layer(const FlowDev& F, int l, const __nv_bf
       part[q] = t;
     }
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
+    for (int q = 0; q < 16; ++q) part[q] += __shfl_xor_sync(0xffffffffu, part[q], 16);
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1) {
       const bool up = (lane & off) != 0;
 #pragma unroll
       for (int i = 0; i < off; ++i) {
@@ -263,7 +266,7 @@ __device__ __forceinline__ void adj_layer(const FlowDev& F, int l, const __nv_bf
         part[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
       }
     }
-    if (r0 + lane < nb) yb[bi[r0 + lane]] += part[0];
+    if (lane < 16 && r0 + lane < nb) yb[bi[r0 + lane]] += part[0];
   }
   __syncwarp();
   if (TRAIN) {
@@ -282,8 +285,14 @@ __device__ __forceinline__ void adj_layer(const FlowDev& F, int l, const __nv_bf
 
 // ---------------------------------------------------------------- the flow kernel
 template <int HPL, int MODE>
-__global__ void __launch_bounds__(128) k_flow(FlowDev F, DevModel M, FlowIO io) {
+__global__ void __launch_bounds__(128) k_flow(FlowDev Fp, DevModel M, FlowIO io) {
   extern __shared__ __align__(16) unsigned char fsm[];
+  // the per-layer tables are indexed by a runtime layer number: from shared
+  // memory, not from a local-memory copy of the parameter block
+  __shared__ FlowDev Fsh;
+  if (threadIdx.x == 0) Fsh = Fp;
+  __syncthreads();
+  const FlowDev& F = Fsh;
   const int T = blockDim.x >> 5;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int d = F.d, H = F.H, L = F.L;
@@ -1033,21 +1042,50 @@ int run_flow_rounds(Model& m, const Flow& f, const Params& P, const Bufs& B, dou
   FL_CUDA(cudaEventCreate(&e1));
   struct EG { cudaEvent_t a, b; ~EG() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
   const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
-  long long graphs = 0;
+  long long graphs = 0, rounds = 0;
+  // every 64th step runs one uncaptured round between events: the kernel durations
+  cudaEvent_t k0, k1, k2;
+  FL_CUDA(cudaEventCreate(&k0));
+  FL_CUDA(cudaEventCreate(&k1));
+  FL_CUDA(cudaEventCreate(&k2));
+  struct KG { cudaEvent_t a, b, c; ~KG() { cudaEventDestroy(a); cudaEventDestroy(b); cudaEventDestroy(c); } } kg{k0, k1, k2};
+  double fsum = 0, asum = 0;
+  int nt = 0;
   FL_CUDA(cudaEventRecord(e0, st));
   for (; graphs < max_graphs; ++graphs) {
-    FL_CUDA(cudaGraphLaunch(exec, st));
+    const bool timed = (graphs & 63) == 5;
+    if (timed) {
+      FL_CUDA(cudaEventRecord(k0, st));
+      if ((rc = launch_flow(f, m.dev, FM_GRAD, io, st, err))) return rc;
+      FL_CUDA(cudaEventRecord(k1, st));
+      k_advance_flow<<<blocks, threads, cache, st>>>(P, B, m.dev, flow_lp.p);
+      FL_CUDA(cudaEventRecord(k2, st));
+      rounds += 1;
+    } else {
+      FL_CUDA(cudaGraphLaunch(exec, st));
+      rounds += ROUNDS;
+    }
     FL_CUDA(cudaMemcpyAsync(h_done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost, st));
     FL_CUDA(cudaStreamSynchronize(st));
+    if (timed && *h_done < P.C) {
+      float a = 0, b = 0;
+      if (cudaEventElapsedTime(&a, k0, k1) == cudaSuccess && cudaEventElapsedTime(&b, k1, k2) == cudaSuccess) {
+        fsum += a;
+        asum += b;
+        ++nt;
+      }
+    }
     if (*h_done >= P.C) break;
   }
   FL_CUDA(cudaEventRecord(e1, st));
   FL_CUDA(cudaEventSynchronize(e1));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
-  stats[0] = (double)(graphs + 1) * ROUNDS;  // rounds
-  stats[1] = ms;                             // device ms
-  stats[2] = (double)(graphs + 1) * ROUNDS * 2;  // launches
+  stats[0] = (double)rounds;
+  stats[1] = ms;               // device ms
+  stats[2] = (double)rounds * 2;  // launches
+  stats[3] = nt ? 1e3 * fsum / nt : 0;  // flow kernel us
+  stats[4] = nt ? 1e3 * asum / nt : 0;  // state-machine kernel us
   return GNUTS_OK;
 }
 

@@ -18,9 +18,9 @@
 // component); a gradient error leaves the leapfrog volume preserving and
 // reversible and lp is computed separately, so it does not bias the target.
 // softplus / inv_logit run in FP32; each thread sums its 32-row slice of lp
-// in FP32 (four interleaved partial sums; the slice's log1p terms as one
-// logarithm of their product) and adds it to an FP64 accumulator; the
-// reduction over row splits is FP64.
+// in FP32 (four interleaved partial sums) and the slices of successive tiles
+// with Kahan-compensated FP32 additions; the reduction over the 512 threads'
+// totals and over row splits is FP64.
 //
 // CTA = one 128-chain tile x one row split, 576 threads:
 //   warp 0       TMA producer: coefficient hi/lo tiles once, X row tiles
@@ -320,7 +320,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       ys[i] = (n < row_end && ((A.ybits[n >> 5] >> (n & 31)) & 1u)) ? 1.f : 0.f;
     }
     asm volatile("bar.sync 1, 512;" ::: "memory");
-    double lp_acc = 0.0;
+    // the slice sums of successive tiles are added in FP32 with Kahan
+    // compensation (no FP64 instruction per tile on this part's narrow FP64
+    // pipe); the thread's total becomes FP64 once, at the end
+    float lp_acc = 0.f, lp_comp = 0.f;
     const int kh = sub >> 1;            // k-half of the R tile this slice lands in
     uint8_t* rrow = smem + OFF_R + kh * HALF_BYTES + cl * 128;
     bool ok = true;
@@ -340,23 +343,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       const float4* y4 = reinterpret_cast<const float4*>(ys + t * 128 + sub * 32);
       const int nvalid = row_end - r0;  // >= 32 on every tile but the last
       float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
-      // products of (1 + e) over 8 elements each: the slice's 32 softplus
-      // logarithms become one lg2 of a product in (1, 2^32]
-      float pr0 = 1.f, pr1 = 1.f, pr2 = 1.f, pr3 = 1.f;
       uint32_t hi[16];
-      // per element: e = exp(-|eta|), softplus(eta) = max(eta, 0) + log1p(e),
-      // inv_logit(eta) from the same e; lp term y eta - softplus(eta), residual
-      // y - inv_logit(eta).  Two MUFU operations per element (ex2, rcp); the
-      // log1p parts are summed as one lg2 of the product of the (1 + e).
-#define GN_EPI_ELEMENT(J, Y, R, ACC, PR)                                           \
+#define GN_EPI_ELEMENT(J, Y, R, ACC)                                               \
       {                                                                            \
         const float eta = v[J];                                                    \
         const float ex = ex2a(-1.4426950408889634f * fabsf(eta));                  \
         const float d = 1.f + ex;                                                  \
+        const float sp = fmaf(lg2a(d), 0.69314718055994531f, fmaxf(eta, 0.f));     \
         const float inv = rcpa(d);                                                 \
         const float sig = (eta >= 0.f ? 1.f : ex) * inv;                           \
-        ACC += fmaf(Y, eta, -fmaxf(eta, 0.f));                                     \
-        PR *= d;                                                                   \
+        ACC += fmaf(Y, eta, -sp);                                                  \
         R = Y - sig;                                                               \
       }
       if (nvalid >= 32) {
@@ -364,15 +360,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         for (int j4 = 0; j4 < 8; ++j4) {
           const float4 yv = y4[j4];
           float r0v, r1v, r2v, r3v;
-          GN_EPI_ELEMENT(4 * j4 + 0, yv.x, r0v, acc0, pr0)
-          GN_EPI_ELEMENT(4 * j4 + 1, yv.y, r1v, acc1, pr1)
-          GN_EPI_ELEMENT(4 * j4 + 2, yv.z, r2v, acc2, pr2)
-          GN_EPI_ELEMENT(4 * j4 + 3, yv.w, r3v, acc3, pr3)
+          GN_EPI_ELEMENT(4 * j4 + 0, yv.x, r0v, acc0)
+          GN_EPI_ELEMENT(4 * j4 + 1, yv.y, r1v, acc1)
+          GN_EPI_ELEMENT(4 * j4 + 2, yv.z, r2v, acc2)
+          GN_EPI_ELEMENT(4 * j4 + 3, yv.w, r3v, acc3)
           hi[2 * j4] = pack_bf16(r0v, r1v);
           hi[2 * j4 + 1] = pack_bf16(r2v, r3v);
         }
       } else {
-        // ragged last tile: rows at or past row_end contribute nothing
 #pragma unroll
         for (int j4 = 0; j4 < 8; ++j4) {
           const float4 yv = y4[j4];
@@ -380,20 +375,23 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const float yy[4] = {yv.x, yv.y, yv.z, yv.w};
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            float a = 0.f, pe = 1.f, r;
-            GN_EPI_ELEMENT(4 * j4 + e, yy[e], r, a, pe)
+            float a = 0.f, r;
+            GN_EPI_ELEMENT(4 * j4 + e, yy[e], r, a)
             const bool valid = 4 * j4 + e < nvalid;
             rv[e] = valid ? r : 0.f;
             acc0 += valid ? a : 0.f;
-            pr0 *= valid ? pe : 1.f;
           }
           hi[2 * j4] = pack_bf16(rv[0], rv[1]);
           hi[2 * j4 + 1] = pack_bf16(rv[2], rv[3]);
         }
       }
 #undef GN_EPI_ELEMENT
-      const float lsp = lg2a((pr0 * pr1) * (pr2 * pr3)) * 0.69314718055994531f;
-      lp_acc += (double)(((acc0 + acc1) + (acc2 + acc3)) - lsp);
+      {
+        const float yk = ((acc0 + acc1) + (acc2 + acc3)) - lp_comp;
+        const float tk = lp_acc + yk;
+        lp_comp = (tk - lp_acc) - yk;
+        lp_acc = tk;
+      }
       // residual buffer t & 1 is free once GEMM2 of tile t - 2 has completed
       if (t >= 2 && !mbar_wait(bar(B_REMPTY + b), ((t >> 1) - 1) & 1, abort)) { ok = false; break; }
       // row cl of the K-major SW128 residual tile: 4 chunks of 8 rows' values
@@ -428,7 +426,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       float* pg = A.part_g + ((size_t)split * A.C + c) * TC_GSTRIDE;
       for (int k = sub; k <= A.K; k += 4) pg[k] = 0.f;
     }
-    lpx[sub * 128 + cl] = lp_acc;
+    lpx[sub * 128 + cl] = (double)lp_acc - (double)lp_comp;
     asm volatile("bar.sync 1, 512;" ::: "memory");
     if (sub == 0 && c < A.C)
       A.part_lp[(size_t)split * A.C + c] = (lpx[cl] + lpx[128 + cl]) + (lpx[256 + cl] + lpx[384 + cl]);

@@ -725,12 +725,14 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   int done = 0;
   RunStats stats;
   if (rc.flow) {
-    double fs[3] = {0, 0, 0};
+    double fs[5] = {0, 0, 0, 0, 0};
     st = run_flow_rounds(m, *rc.flow, P, B, per_chain_max, fs, err);
     if (st) return st;
     stats.rounds = fs[0];
     stats.device_ms = fs[1];
     stats.launches = fs[2];
+    stats.grad_us = fs[3];
+    stats.advance_us = fs[4];
     GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
     if (done >= C) {
       st = flow_finalize_draws(m, *rc.flow, C * P.n_saved, B.zdraws, B.draws, P.ncol, err);

@@ -283,6 +283,21 @@ def test_seed_determinism():
     assert np.array_equal(a.draws, b.draws)
 
 
+def test_autotuned_launch_shape_does_not_change_draws():
+    """With 64 chains or more the fused driver times several launch shapes
+    (chains per CTA, shared-memory cache) on the run's first gradients and
+    keeps the fastest; every chain computes the same numbers under any shape,
+    so runs are bitwise reproducible and equal to each chain run alone."""
+    gm = gn.Model("hier", workloads.eight_schools())
+    a = gm.sample(num_chains=96, seed=21, num_warmup=150, num_samples=60)
+    b = gm.sample(num_chains=96, seed=21, num_warmup=150, num_samples=60)
+    assert a.timing["chains_per_cta"] in (1, 2, 4)
+    assert np.array_equal(a.draws, b.draws)
+    # chain 40 alone (below the tuning threshold: the default shape) gives the same draws
+    solo = gm.sample(num_chains=1, chain_id=41, seed=21, num_warmup=150, num_samples=60)
+    assert np.array_equal(solo.draws[0], a.draws[40])
+
+
 def test_chain_ids_offset_draws():
     gm = gn.Model("proper")
     a = gm.sample(num_chains=3, chain_id=10, seed=5, num_warmup=50, num_samples=20)

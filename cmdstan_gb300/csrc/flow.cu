@@ -433,6 +433,126 @@ __global__ void __launch_bounds__(128) k_flow(FlowDev Fp, DevModel M, FlowIO io)
   }
 }
 
+// ---------------------------------------------------------------- fused NUTS in the pulled-back space
+// One pass of the gradient pipeline for the CTA's T points: each live warp's
+// point z (FP64, d values) goes through the forward stages, the model and the
+// adjoint stages; g (FP64) receives the gradient in z and the return value is
+// lp_x(T(z)) + log|det|.  Every warp of the CTA calls it (the weight stages
+// are CTA-wide); warps with live == false only take part in the barriers.
+template <int HPL>
+__device__ double flow_grad_pass(const FlowDev& F, const DevModel& M, unsigned char* fsm, const int* sidx,
+                                 __nv_bfloat16* wbuf0, __nv_bfloat16* wbuf1, unsigned char* wr, bool live,
+                                 const double* z, double* g, int lane) {
+  const int d = F.d, H = F.H, L = F.L;
+  const int namax = flow_namax(F);
+  double* x = reinterpret_cast<double*>(wr);
+  double* gx = x + d;
+  float* y = reinterpret_cast<float*>(gx + d);
+  float* yb = y + d;
+  float* sc = yb + d;
+  const int scn = 2 * namax > H ? 2 * namax : H;
+  float* pb = sc + scn;
+  float* tape = pb + H;
+  float* uL = tape + tape_off(F, L);
+  issue_stage(F, 0, wbuf0);
+  fl_commit();
+  double ld = 0, lp = 0;
+  if (live)
+    for (int i = lane; i < d; i += 32) y[i] = (float)z[i];
+  __syncwarp();
+  const float* mu = F.theta + F.th_off[L];
+  const float* rho = F.theta + F.th_rho;
+  const int S = 2 * L;
+  for (int st = 0; st < S; ++st) {
+    if (st + 1 < S) {
+      issue_stage(F, st + 1, (st + 1) & 1 ? wbuf1 : wbuf0);
+      fl_commit();
+      fl_wait<1>();
+    } else {
+      fl_wait<0>();
+    }
+    __syncthreads();
+    const __nv_bfloat16* buf = st & 1 ? wbuf1 : wbuf0;
+    if (live) {
+      if (st < L) {
+        const int to = tape_off(F, st);
+        fwd_layer<HPL>(F, st, buf, sidx + st * d, sidx + st * d + F.nb[st], y, tape + to, tape + to + d,
+                       tape + to + d + H, sc, ld, lane);
+      } else {
+        if (st == L) {
+          for (int i = lane; i < d; i += 32) {
+            uL[i] = y[i];
+            x[i] = (double)mu[i] + exp((double)rho[i]) * (double)y[i];
+            ld += (double)rho[i];
+          }
+          __syncwarp();
+          const double lpx = warp_log_prob_grad(M, x, gx, 1, lane);
+          __syncwarp();
+          lp = lpx + wsum(ld);
+          for (int i = lane; i < d; i += 32) yb[i] = (float)(gx[i] * exp((double)rho[i]));
+          __syncwarp();
+        }
+        const int l = 2 * L - 1 - st;
+        const int to = tape_off(F, l);
+        adj_layer<HPL, false>(F, l, buf, sidx + l * d, sidx + l * d + F.nb[l], yb, tape + to, tape + to + d,
+                              tape + to + d + H, sc, pb, nullptr, lane);
+      }
+    }
+    __syncthreads();
+  }
+  if (live) {
+    for (int i = lane; i < d; i += 32) g[i] = (double)yb[i];
+    __syncwarp();
+  }
+  return lp;
+}
+
+// Fused flow sampler: each warp runs one chain's NUTS state machine on z and
+// evaluates its gradients through the flow itself, up to P.grad_budget
+// gradients per launch, with the chain's vectors cached in shared memory
+// behind the flow's buffers when they fit (P.cache, cache_stride per warp).
+template <int HPL>
+__global__ void __launch_bounds__(128) k_fused_flow(FlowDev Fp, Params P, Bufs B, DevModel M, size_t flow_bytes) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  __shared__ FlowDev Fsh;
+  if (threadIdx.x == 0) Fsh = Fp;
+  __syncthreads();
+  const FlowDev& F = Fsh;
+  const int T = blockDim.x >> 5;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int d = F.d, L = F.L;
+  const int namax = flow_namax(F);
+  const size_t idx_bytes = flow_align16(sizeof(int) * (size_t)L * d);
+  const size_t wbuf_bytes = flow_align16(2 * (size_t)F.stage_max);
+  const size_t warp_bytes = flow_warp_bytes(F, namax);
+  int* sidx = reinterpret_cast<int*>(fsm);
+  __nv_bfloat16* wbuf0 = reinterpret_cast<__nv_bfloat16*>(fsm + idx_bytes);
+  __nv_bfloat16* wbuf1 = reinterpret_cast<__nv_bfloat16*>(fsm + idx_bytes + wbuf_bytes);
+  unsigned char* wr = fsm + idx_bytes + 2 * wbuf_bytes + (size_t)w * warp_bytes;
+  for (int i = threadIdx.x; i < L * d; i += blockDim.x) sidx[i] = F.idx[i];
+  const int c = blockIdx.x * T + w;
+  const bool exists = c < P.C;
+  Scal s;
+  if (exists) s = B.sc[c];
+  bool live = exists && s.phase < PH_DONE;
+  const bool attached = live && P.cache;
+  Chain ch(P, B, M, s, exists ? c : 0, lane);
+  double* cache = reinterpret_cast<double*>(fsm + flow_bytes) + (size_t)w * P.cache_stride;
+  if (attached) ch.cache_attach(cache);
+  for (int b = 0; b < P.grad_budget; ++b) {
+    if (!__syncthreads_or(live)) break;
+    const double lp = flow_grad_pass<HPL>(F, M, fsm, sidx, wbuf0, wbuf1, wr, live, ch.Wq, ch.Wg, lane);
+    if (live) {
+      s.W_lp = lp;
+      __syncwarp();
+      live = ch.advance();
+    }
+  }
+  if (attached) ch.cache_detach();
+  __syncwarp();
+  if (exists && lane == 0) B.sc[c] = s;
+}
+
 // ---------------------------------------------------------------- inverse
 // x -> z, one warp per point, weights read from global memory (used once per
 // chain to map starting points into the pulled-back space)
@@ -1111,6 +1231,83 @@ int flow_inverse_device(const Flow& f, int n, const double* dx, double* dz, std:
   int rc = launch_inverse(f, n, dx, dz, nullptr, err);
   if (rc) return rc;
   FL_CUDA(cudaDeviceSynchronize());
+  return GNUTS_OK;
+}
+
+int run_flow_fused(Model& m, const Flow& f, Params& P, const Bufs& B, double per_chain_max, double* stats,
+                   std::string& err) {
+  if (P.ld != ((f.d + 3) & ~3) || P.D != f.d) {
+    err = "flow / sampler dimension mismatch";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  const FlowDev F = dev_of(f);
+  // CTA shape: the largest T in {4, 2, 1} whose flow buffers plus (if they fit)
+  // the T chains' cached vectors stay within the shared-memory budget
+  const size_t chain_bytes = (size_t)P.cache_stride * sizeof(double);
+  int T = 0;
+  size_t flow_bytes = 0;
+  bool cache = false;
+  for (int t = 4; t >= 1 && !T; t >>= 1) {
+    FlowPlan pl = flow_plan(F, FLOW_SMEM_LIMIT);
+    if (pl.T == 0) break;
+    const size_t fb = pl.idx_bytes + 2 * pl.wbuf_bytes + (size_t)t * pl.warp_bytes;
+    if (fb + (size_t)t * chain_bytes <= FLOW_SMEM_LIMIT) {
+      T = t;
+      flow_bytes = fb;
+      cache = true;
+    } else if (t == 1 && fb <= FLOW_SMEM_LIMIT) {
+      T = 1;
+      flow_bytes = fb;
+      cache = false;
+    }
+  }
+  if (!T) {
+    err = "flow does not fit in shared memory";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  P.cache = cache ? 1 : 0;
+  const size_t smem = flow_align16(flow_bytes) + (cache ? (size_t)T * chain_bytes : 0);
+  flow_bytes = flow_align16(flow_bytes);
+  const int blocks = (P.C + T - 1) / T;
+  switch (f.H) {
+    case 128: FL_CUDA(cudaFuncSetAttribute(k_fused_flow<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); break;
+    case 64: FL_CUDA(cudaFuncSetAttribute(k_fused_flow<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); break;
+    default: FL_CUDA(cudaFuncSetAttribute(k_fused_flow<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); break;
+  }
+  FL_CUDA(cudaDeviceSynchronize());  // k_init done
+  int* h_done = nullptr;
+  FL_CUDA(cudaMallocHost(&h_done, sizeof(int)));
+  struct HG { int* p; ~HG() { cudaFreeHost(p); } } hg{h_done};
+  cudaEvent_t e0, e1;
+  FL_CUDA(cudaEventCreate(&e0));
+  FL_CUDA(cudaEventCreate(&e1));
+  struct EG { cudaEvent_t a, b; ~EG() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
+  const long long max_launches = (long long)(per_chain_max / P.grad_budget) + 16;
+  long long launches = 0;
+  FL_CUDA(cudaEventRecord(e0));
+  for (; launches < max_launches; ++launches) {
+    switch (f.H) {
+      case 128: k_fused_flow<4><<<blocks, 32 * T, smem>>>(F, P, B, m.dev, flow_bytes); break;
+      case 64: k_fused_flow<2><<<blocks, 32 * T, smem>>>(F, P, B, m.dev, flow_bytes); break;
+      default: k_fused_flow<1><<<blocks, 32 * T, smem>>>(F, P, B, m.dev, flow_bytes); break;
+    }
+    FL_CUDA(cudaGetLastError());
+    FL_CUDA(cudaMemcpy(h_done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
+    if (*h_done >= P.C) {
+      ++launches;
+      break;
+    }
+  }
+  FL_CUDA(cudaEventRecord(e1));
+  FL_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  stats[0] = (double)launches;
+  stats[1] = ms;
+  stats[2] = (double)launches;
+  stats[3] = 0;
+  stats[4] = launches ? 1e3 * ms / launches : 0;
+  stats[5] = T;
   return GNUTS_OK;
 }
 

@@ -575,6 +575,8 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
 // flow.cu
 int run_flow_rounds(Model& m, const Flow& f, const Params& P, const Bufs& B, double per_chain_max, double* stats,
                     std::string& err);
+int run_flow_fused(Model& m, const Flow& f, Params& P, const Bufs& B, double per_chain_max, double* stats,
+                   std::string& err);
 int flow_finalize_draws(Model& m, const Flow& f, int rows, const double* zdraws, double* draws, int ncol,
                         std::string& err);
 
@@ -725,14 +727,15 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   int done = 0;
   RunStats stats;
   if (rc.flow) {
-    double fs[5] = {0, 0, 0, 0, 0};
-    st = run_flow_rounds(m, *rc.flow, P, B, per_chain_max, fs, err);
+    double fs[6] = {0, 0, 0, 0, 0, 4};
+    st = run_flow_fused(m, *rc.flow, P, B, per_chain_max, fs, err);
     if (st) return st;
     stats.rounds = fs[0];
     stats.device_ms = fs[1];
     stats.launches = fs[2];
     stats.grad_us = fs[3];
     stats.advance_us = fs[4];
+    stats.chains_per_cta = fs[5];
     GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
     if (done >= C) {
       st = flow_finalize_draws(m, *rc.flow, C * P.n_saved, B.zdraws, B.draws, P.ncol, err);

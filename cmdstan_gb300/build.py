@@ -25,7 +25,10 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "-I" + INC, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-I" + CSRC]
 
-CU_SOURCES = ["sampler.cu", "grad_tc.cu", "noalloc.cu", "flow.cu", "summary_gpu.cu"]
+CU_SOURCES = ["sampler.cu", "fused.cu", "grad_tc.cu", "noalloc.cu", "flow.cu", "summary_gpu.cu"]
+# compiled once per model kind (-DGNUTS_KIND=k, k = 0..N_KINDS-1)
+CU_KIND_SOURCES = ["fused_kind.cu", "flow_tc_kind.cu"]
+N_KINDS = 7
 CPP_SOURCES = ["abi.cpp", "summary.cpp", "learned.cpp"]
 
 
@@ -75,6 +78,13 @@ def build(verbose=False, jobs=None):
         objs.append(o)
         if _newer(o, [s] + headers):
             cmds.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
+    for src in CU_KIND_SOURCES:
+        s = os.path.join(CSRC, src)
+        for k in range(N_KINDS):
+            o = os.path.join(objdir, "%s.k%d.o" % (src, k))
+            objs.append(o)
+            if _newer(o, [s] + headers):
+                cmds.append([nvcc] + NVCC_FLAGS + ["-DGNUTS_KIND=%d" % k, "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(objdir, src + ".o")
@@ -83,7 +93,7 @@ def build(verbose=False, jobs=None):
             cmds.append(["g++"] + CXX_FLAGS + ["-I" + os.path.join(cuda, "include"), "-c", s, "-o", o])
     # oracle (test infrastructure) builds alongside
     oracle_cmd = ["make", "-s", "-C", ORACLE]
-    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(cmds) + 1)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(os.cpu_count() or 8, len(cmds) + 1)) as ex:
         futs = [ex.submit(_run, c) for c in cmds] + [ex.submit(_run, oracle_cmd)]
         for f in futs:
             out = f.result()

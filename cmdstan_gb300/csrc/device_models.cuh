@@ -378,6 +378,19 @@ __device__ __forceinline__ double warp_log_prob_grad(const DevModel& M, const do
   return __longlong_as_double(0x7ff8000000000000ll);
 }
 
+// the same for a model kind known at compile time (kernels instantiated per
+// kind carry only that model's code)
+template <int KIND>
+__device__ __forceinline__ double warp_lpg_k(const DevModel& M, const double* q, double* g, int jac, int lane) {
+  if constexpr (KIND == MK_BERNOULLI) return lpg_bernoulli(M, q, g, jac, lane);
+  else if constexpr (KIND == MK_NORMAL) return lpg_normal(M, q, g, jac, lane);
+  else if constexpr (KIND == MK_LOGISTIC) return lpg_logistic(M, q, g, jac, lane);
+  else if constexpr (KIND == MK_HIER) return lpg_hier(M, q, g, jac, lane);
+  else if constexpr (KIND == MK_FUNNEL) return lpg_funnel(M, q, g, jac, lane);
+  else if constexpr (KIND == MK_VARINT) return lpg_varint(M, q, g, jac, lane);
+  else return lpg_horseshoe(M, q, g, jac, lane);
+}
+
 // the model a chain (or point) c of C evaluates: itself, or its posterior-set member
 __device__ __forceinline__ const DevModel& chain_model(const DevModel& M, int c, int C) {
   return M.members ? M.members[c / (C / M.n_members)] : M;

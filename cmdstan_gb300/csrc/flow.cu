@@ -76,13 +76,6 @@ __device__ __forceinline__ void ld_bf(const __nv_bfloat16* p, float* f) {
   }
 }
 
-__device__ __forceinline__ void fl_cp16(void* s, const void* g) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(s)), "l"(g)
-               : "memory");
-}
-__device__ __forceinline__ void fl_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void fl_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // stage s < L: forward layer s -> [W2 | W1]; stage s >= L: adjoint layer 2L-1-s -> [W1 | W2^T]
 __device__ __forceinline__ void issue_stage(const FlowDev& F, int s, __nv_bfloat16* buf) {
@@ -433,126 +426,6 @@ __global__ void __launch_bounds__(128) k_flow(FlowDev Fp, DevModel M, FlowIO io)
   }
 }
 
-// ---------------------------------------------------------------- fused NUTS in the pulled-back space
-// One pass of the gradient pipeline for the CTA's T points: each live warp's
-// point z (FP64, d values) goes through the forward stages, the model and the
-// adjoint stages; g (FP64) receives the gradient in z and the return value is
-// lp_x(T(z)) + log|det|.  Every warp of the CTA calls it (the weight stages
-// are CTA-wide); warps with live == false only take part in the barriers.
-template <int HPL>
-__device__ double flow_grad_pass(const FlowDev& F, const DevModel& M, unsigned char* fsm, const int* sidx,
-                                 __nv_bfloat16* wbuf0, __nv_bfloat16* wbuf1, unsigned char* wr, bool live,
-                                 const double* z, double* g, int lane) {
-  const int d = F.d, H = F.H, L = F.L;
-  const int namax = flow_namax(F);
-  double* x = reinterpret_cast<double*>(wr);
-  double* gx = x + d;
-  float* y = reinterpret_cast<float*>(gx + d);
-  float* yb = y + d;
-  float* sc = yb + d;
-  const int scn = 2 * namax > H ? 2 * namax : H;
-  float* pb = sc + scn;
-  float* tape = pb + H;
-  float* uL = tape + tape_off(F, L);
-  issue_stage(F, 0, wbuf0);
-  fl_commit();
-  double ld = 0, lp = 0;
-  if (live)
-    for (int i = lane; i < d; i += 32) y[i] = (float)z[i];
-  __syncwarp();
-  const float* mu = F.theta + F.th_off[L];
-  const float* rho = F.theta + F.th_rho;
-  const int S = 2 * L;
-  for (int st = 0; st < S; ++st) {
-    if (st + 1 < S) {
-      issue_stage(F, st + 1, (st + 1) & 1 ? wbuf1 : wbuf0);
-      fl_commit();
-      fl_wait<1>();
-    } else {
-      fl_wait<0>();
-    }
-    __syncthreads();
-    const __nv_bfloat16* buf = st & 1 ? wbuf1 : wbuf0;
-    if (live) {
-      if (st < L) {
-        const int to = tape_off(F, st);
-        fwd_layer<HPL>(F, st, buf, sidx + st * d, sidx + st * d + F.nb[st], y, tape + to, tape + to + d,
-                       tape + to + d + H, sc, ld, lane);
-      } else {
-        if (st == L) {
-          for (int i = lane; i < d; i += 32) {
-            uL[i] = y[i];
-            x[i] = (double)mu[i] + exp((double)rho[i]) * (double)y[i];
-            ld += (double)rho[i];
-          }
-          __syncwarp();
-          const double lpx = warp_log_prob_grad(M, x, gx, 1, lane);
-          __syncwarp();
-          lp = lpx + wsum(ld);
-          for (int i = lane; i < d; i += 32) yb[i] = (float)(gx[i] * exp((double)rho[i]));
-          __syncwarp();
-        }
-        const int l = 2 * L - 1 - st;
-        const int to = tape_off(F, l);
-        adj_layer<HPL, false>(F, l, buf, sidx + l * d, sidx + l * d + F.nb[l], yb, tape + to, tape + to + d,
-                              tape + to + d + H, sc, pb, nullptr, lane);
-      }
-    }
-    __syncthreads();
-  }
-  if (live) {
-    for (int i = lane; i < d; i += 32) g[i] = (double)yb[i];
-    __syncwarp();
-  }
-  return lp;
-}
-
-// Fused flow sampler: each warp runs one chain's NUTS state machine on z and
-// evaluates its gradients through the flow itself, up to P.grad_budget
-// gradients per launch, with the chain's vectors cached in shared memory
-// behind the flow's buffers when they fit (P.cache, cache_stride per warp).
-template <int HPL>
-__global__ void __launch_bounds__(128) k_fused_flow(FlowDev Fp, Params P, Bufs B, DevModel M, size_t flow_bytes) {
-  extern __shared__ __align__(16) unsigned char fsm[];
-  __shared__ FlowDev Fsh;
-  if (threadIdx.x == 0) Fsh = Fp;
-  __syncthreads();
-  const FlowDev& F = Fsh;
-  const int T = blockDim.x >> 5;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int d = F.d, L = F.L;
-  const int namax = flow_namax(F);
-  const size_t idx_bytes = flow_align16(sizeof(int) * (size_t)L * d);
-  const size_t wbuf_bytes = flow_align16(2 * (size_t)F.stage_max);
-  const size_t warp_bytes = flow_warp_bytes(F, namax);
-  int* sidx = reinterpret_cast<int*>(fsm);
-  __nv_bfloat16* wbuf0 = reinterpret_cast<__nv_bfloat16*>(fsm + idx_bytes);
-  __nv_bfloat16* wbuf1 = reinterpret_cast<__nv_bfloat16*>(fsm + idx_bytes + wbuf_bytes);
-  unsigned char* wr = fsm + idx_bytes + 2 * wbuf_bytes + (size_t)w * warp_bytes;
-  for (int i = threadIdx.x; i < L * d; i += blockDim.x) sidx[i] = F.idx[i];
-  const int c = blockIdx.x * T + w;
-  const bool exists = c < P.C;
-  Scal s;
-  if (exists) s = B.sc[c];
-  bool live = exists && s.phase < PH_DONE;
-  const bool attached = live && P.cache;
-  Chain ch(P, B, M, s, exists ? c : 0, lane);
-  double* cache = reinterpret_cast<double*>(fsm + flow_bytes) + (size_t)w * P.cache_stride;
-  if (attached) ch.cache_attach(cache);
-  for (int b = 0; b < P.grad_budget; ++b) {
-    if (!__syncthreads_or(live)) break;
-    const double lp = flow_grad_pass<HPL>(F, M, fsm, sidx, wbuf0, wbuf1, wr, live, ch.Wq, ch.Wg, lane);
-    if (live) {
-      s.W_lp = lp;
-      __syncwarp();
-      live = ch.advance();
-    }
-  }
-  if (attached) ch.cache_detach();
-  __syncwarp();
-  if (exists && lane == 0) B.sc[c] = s;
-}
-
 // ---------------------------------------------------------------- inverse
 // x -> z, one warp per point, weights read from global memory (used once per
 // chain to map starting points into the pulled-back space)
@@ -618,24 +491,34 @@ __device__ __forceinline__ int flow_decode(const FlowDev& F, long i, int& l, int
 
 // BF16 copies of weight parameter i (forward and transposed layouts)
 __device__ __forceinline__ void flow_put_w16(const FlowDev& F, int kind, int l, int a, int b, float v,
-                                             __nv_bfloat16* w16) {
+                                             __nv_bfloat16* w16, __nv_bfloat16* w16t) {
   if (kind != 0 && kind != 2) return;
   const long H = F.H, nb = F.nb[l], n2 = 2 * (long)F.na[l];
   __nv_bfloat16* blk = w16 + F.w_off[l];
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  // tensor-core blocks: F1 [H][kb+8], F2 [ma][H+8], A3 [H][ma+8], A4 [kb][H+8]
+  const long sb = tc_pad16((int)nb) + 8, sa = tc_pad16((int)n2) + 8, sh = H + 8;
+  __nv_bfloat16* f1 = w16t + F.wt_off[l];
+  __nv_bfloat16* f2 = f1 + H * sb;
+  __nv_bfloat16* a3 = f2 + (long)tc_pad16((int)n2) * sh;
+  __nv_bfloat16* a4 = a3 + H * sa;
   if (kind == 0) {
     blk[H * n2 + (long)a * H + b] = h;  // W1 [r][j]
+    f1[(long)b * sb + a] = h;
+    a4[(long)a * sh + b] = h;
   } else {
     blk[(long)a * n2 + b] = h;                // W2 [j][m]
     blk[H * n2 + nb * H + (long)b * H + a] = h;  // W2^T [m][j]
+    f2[(long)b * sh + a] = h;
+    a3[(long)a * sa + b] = h;
   }
 }
 
-__global__ void k_flow_sync_w16(FlowDev F, __nv_bfloat16* w16) {
+__global__ void k_flow_sync_w16(FlowDev F, __nv_bfloat16* w16, __nv_bfloat16* w16t) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < F.th_off[F.L]; i += (long)gridDim.x * blockDim.x) {
     int l, a, b;
     const int kind = flow_decode(F, i, l, a, b);
-    flow_put_w16(F, kind, l, a, b, F.theta[i], w16);
+    flow_put_w16(F, kind, l, a, b, F.theta[i], w16, w16t);
   }
 }
 
@@ -678,7 +561,8 @@ __global__ void k_flow_pgrad(FlowDev F, int n, const float* fac, const int* vali
 // given (gradient of the mean loss), else 1.  Weight matrices are re-rounded
 // into their BF16 copies.
 __global__ void k_flow_adam(FlowDev F, float* theta, float* m, float* v, const float* grad, const int* nvalid,
-                            int t, float lr, float b1, float b2, float eps, __nv_bfloat16* w16) {
+                            int t, float lr, float b1, float b2, float eps, __nv_bfloat16* w16,
+                            __nv_bfloat16* w16t) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= F.n_params) return;
   float scale = 1.0f;
@@ -697,7 +581,7 @@ __global__ void k_flow_adam(FlowDev F, float* theta, float* m, float* v, const f
   theta[i] = th;
   int l, a, b;
   const int kind = flow_decode(F, i, l, a, b);
-  flow_put_w16(F, kind, l, a, b, th, w16);
+  flow_put_w16(F, kind, l, a, b, th, w16, w16t);
 }
 
 __global__ void k_flow_loss_mean(int n, const float* loss, const int* valid, double* out) {
@@ -725,7 +609,8 @@ __global__ void k_flow_loss_mean(int n, const float* loss, const int* valid, dou
 
 // ---------------------------------------------------------------- host side
 Flow::~Flow() {
-  for (void* p : {(void*)theta, (void*)adam_m, (void*)adam_v, (void*)grad, (void*)w16, (void*)didx, (void*)nvalid})
+  for (void* p : {(void*)theta, (void*)adam_m, (void*)adam_v, (void*)grad, (void*)w16, (void*)w16t, (void*)didx,
+                  (void*)nvalid})
     if (p) cudaFree(p);
 }
 
@@ -748,9 +633,12 @@ FlowDev dev_of(const Flow& f) {
   F.th_rho = f.th_rho;
   F.n_params = f.n_params;
   F.stage_max = f.stage_max;
+  for (int l = 0; l < f.L; ++l) F.wt_off[l] = f.wt_off[l];
+  F.stage_max_tc = f.stage_max_tc;
   F.idx = f.didx;
   F.theta = f.theta;
   F.w16 = reinterpret_cast<const __nv_bfloat16*>(f.w16);
+  F.w16t = reinterpret_cast<const __nv_bfloat16*>(f.w16t);
   return F;
 }
 
@@ -766,6 +654,8 @@ int ensure_flow_device(Flow& f, std::string& err) {
   FL_CUDA(cudaMalloc(&f.adam_v, sizeof(float) * f.n_params));
   FL_CUDA(cudaMalloc(&f.grad, sizeof(float) * f.n_params));
   FL_CUDA(cudaMalloc(&f.w16, sizeof(uint16_t) * f.n_w16));
+  FL_CUDA(cudaMalloc(&f.w16t, sizeof(uint16_t) * f.n_w16t));
+  FL_CUDA(cudaMemset(f.w16t, 0, sizeof(uint16_t) * f.n_w16t));  // padding stays zero
   FL_CUDA(cudaMalloc(&f.didx, sizeof(int) * f.idx.size()));
   FL_CUDA(cudaMalloc(&f.nvalid, sizeof(int) * 2));
   FL_CUDA(cudaMemset(f.theta, 0, sizeof(float) * f.n_params));
@@ -790,6 +680,32 @@ struct DevBuf {
 };
 
 constexpr size_t FLOW_SMEM_LIMIT = 220 * 1024;
+
+#define FLOW_KIND_SWITCH(kind, CALL)               \
+  switch (kind) {                                  \
+    case MK_BERNOULLI: return CALL(MK_BERNOULLI);   \
+    case MK_NORMAL: return CALL(MK_NORMAL);         \
+    case MK_LOGISTIC: return CALL(MK_LOGISTIC);     \
+    case MK_HIER: return CALL(MK_HIER);             \
+    case MK_FUNNEL: return CALL(MK_FUNNEL);         \
+    case MK_VARINT: return CALL(MK_VARINT);         \
+    case MK_HORSESHOE: return CALL(MK_HORSESHOE);   \
+  }                                                \
+  return cudaErrorInvalidValue
+
+cudaError_t flow_tc_fused_launch(int kind, const FlowDev& F, const Params& P, const Bufs& B, const DevModel& M,
+                                 int T, size_t flow_bytes, int blocks, size_t smem) {
+#define CALL(K) flow_tc_fused_launch_k<K>(F, P, B, M, T, flow_bytes, blocks, smem)
+  FLOW_KIND_SWITCH(kind, CALL);
+#undef CALL
+}
+
+cudaError_t flow_tc_grad_launch(int kind, const FlowDev& F, const DevModel& M, int n, int T, const double* z,
+                                double* lp, double* g, size_t smem) {
+#define CALL(K) flow_tc_grad_launch_k<K>(F, M, n, T, z, lp, g, smem)
+  FLOW_KIND_SWITCH(kind, CALL);
+#undef CALL
+}
 
 // shared-memory opt-in of the flow kernels for this flow's plan; called
 // before any launch (and outside stream capture)
@@ -880,6 +796,10 @@ int flow_create(int d, int L, int H, double clamp, Flow** out, std::string& err)
     f->w_off.push_back(wo);
     wo += (long)H * n2 + nb * H + n2 * H;
     f->stage_max = std::max<int>(f->stage_max, (int)((long)H * n2 + nb * H));
+    const long tf = tc_fwd_elems(H, (int)nb, (int)a.size()), ta = tc_adj_elems(H, (int)nb, (int)a.size());
+    f->wt_off.push_back(f->n_w16t);
+    f->n_w16t += tf + ta;
+    f->stage_max_tc = std::max<int>(f->stage_max_tc, (int)std::max(tf, ta));
   }
   f->th_off.push_back(o);
   f->th_rho = o + d;
@@ -898,7 +818,8 @@ int flow_set_params(Flow& f, const double* theta, std::string& err) {
   FL_CUDA(cudaMemset(f.adam_m, 0, sizeof(float) * f.n_params));
   FL_CUDA(cudaMemset(f.adam_v, 0, sizeof(float) * f.n_params));
   const FlowDev F = dev_of(f);
-  k_flow_sync_w16<<<256, 256>>>(F, reinterpret_cast<__nv_bfloat16*>(f.w16));
+  k_flow_sync_w16<<<256, 256>>>(F, reinterpret_cast<__nv_bfloat16*>(f.w16),
+                                reinterpret_cast<__nv_bfloat16*>(f.w16t));
   FL_CUDA(cudaGetLastError());
   FL_CUDA(cudaDeviceSynchronize());
   return GNUTS_OK;
@@ -1024,6 +945,34 @@ int flow_log_prob_grad(Model& m, Flow& f, int n, const double* z, int jacobian, 
   return GNUTS_OK;
 }
 
+int flow_log_prob_grad_tc(Model& m, Flow& f, int n, const double* z, double* lp, double* grad_z,
+                          std::string& err) {
+  int rc = upload(m, err);
+  if (rc) return rc;
+  if (m.dev.D != f.d) {
+    err = "flow dimension does not match the model's";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  if ((rc = ensure_flow_device(f, err)) || n <= 0) return rc;
+  const FlowDev F = dev_of(f);
+  int T = 8;
+  while (T > 1 && flow_tc_bytes(F, T) > FLOW_SMEM_LIMIT) T >>= 1;
+  const size_t smem = flow_tc_bytes(F, T);
+  if (smem > FLOW_SMEM_LIMIT) {
+    err = "flow does not fit in shared memory";
+    return GNUTS_ERR_ARGUMENT;
+  }
+  DevBuf<double> dz, dg, dl;
+  FL_CUDA(dz.alloc((size_t)n * f.d));
+  FL_CUDA(dg.alloc((size_t)n * f.d));
+  FL_CUDA(dl.alloc(n));
+  FL_CUDA(cudaMemcpy(dz.p, z, sizeof(double) * n * f.d, cudaMemcpyHostToDevice));
+  FL_CUDA(flow_tc_grad_launch(m.dev.kind, F, m.dev, n, T, dz.p, dl.p, dg.p, smem));
+  FL_CUDA(cudaMemcpy(lp, dl.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  FL_CUDA(cudaMemcpy(grad_z, dg.p, sizeof(double) * n * f.d, cudaMemcpyDeviceToHost));
+  return GNUTS_OK;
+}
+
 int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, double b2, double eps,
                    std::string& err) {
   int rc = ensure_flow_device(f, err);
@@ -1034,7 +983,8 @@ int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, dou
   const FlowDev F = dev_of(f);
   k_flow_adam<<<(int)((f.n_params + 255) / 256), 256>>>(F, f.theta, f.adam_m, f.adam_v, f.grad, nullptr, t,
                                                        (float)lr, (float)b1, (float)b2, (float)eps,
-                                                       reinterpret_cast<__nv_bfloat16*>(f.w16));
+                                                       reinterpret_cast<__nv_bfloat16*>(f.w16),
+                                                       reinterpret_cast<__nv_bfloat16*>(f.w16t));
   FL_CUDA(cudaGetLastError());
   FL_CUDA(cudaDeviceSynchronize());
   return GNUTS_OK;
@@ -1083,129 +1033,13 @@ int flow_train(Model& m, Flow& f, const gnuts_train_args& ta, double* loss_trace
     // learning rate decays linearly to a tenth of its start over the run
     const float lr_t = (float)(lr * (1.0 - 0.9 * (double)(t - 1) / (double)steps));
     k_flow_adam<<<pblocks, 256>>>(F, f.theta, f.adam_m, f.adam_v, f.grad, f.nvalid, t, lr_t, 0.9f, 0.999f, 1e-8f,
-                                  reinterpret_cast<__nv_bfloat16*>(f.w16));
+                                  reinterpret_cast<__nv_bfloat16*>(f.w16),
+                                  reinterpret_cast<__nv_bfloat16*>(f.w16t));
     k_flow_loss_mean<<<1, 256>>>(batch, loss.p, valid.p, trace.p + (t - 1));
     FL_CUDA(cudaGetLastError());
   }
   FL_CUDA(cudaDeviceSynchronize());
   if (loss_trace) FL_CUDA(cudaMemcpy(loss_trace, trace.p, sizeof(double) * steps, cudaMemcpyDeviceToHost));
-  return GNUTS_OK;
-}
-
-// ---------------------------------------------------------------- NUTS in the pulled-back space
-// The state machine of nuts_device.cuh samples z; every round the flow kernel
-// (FM_GRAD) turns each live chain's requested point into lp_x(T(z)) +
-// log|det| and its gradient in z, written straight into the chain's W.g.
-__global__ void __launch_bounds__(128) k_advance_flow(Params P, Bufs B, DevModel M, const double* flow_lp) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= P.C) return;
-  Scal s = B.sc[warp];
-  if (s.phase >= PH_DONE) return;
-  Chain ch(P, B, M, s, warp, lane);
-  extern __shared__ double gn_cache[];
-  if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
-  s.W_lp = flow_lp[warp];
-  __syncwarp();
-  ch.advance();
-  if (P.cache) ch.cache_detach();
-  __syncwarp();
-  if (lane == 0) B.sc[warp] = s;
-}
-
-int run_flow_rounds(Model& m, const Flow& f, const Params& P, const Bufs& B, double per_chain_max, double* stats,
-                    std::string& err) {
-  if (P.ld != ((f.d + 3) & ~3) || P.D != f.d) {
-    err = "flow / sampler dimension mismatch";
-    return GNUTS_ERR_ARGUMENT;
-  }
-  DevBuf<double> flow_lp;
-  FL_CUDA(flow_lp.alloc(P.C));
-  cudaStream_t st;
-  FL_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  struct SG { cudaStream_t s; ~SG() { cudaStreamDestroy(s); } } sg{st};
-  FlowIO io{};
-  io.n = P.C;
-  io.z = B.Wq;
-  io.ldz = P.ld;
-  io.sc = B.sc;
-  io.jac = 1;
-  io.lp = flow_lp.p;
-  io.g = B.Wg;
-  io.ldg = P.ld;
-  const int threads = 128, blocks = (P.C * 32 + threads - 1) / threads;
-  const size_t cache = P.cache ? 4 * (size_t)P.cache_stride * sizeof(double) : 0;
-  if (P.cache)
-    FL_CUDA(cudaFuncSetAttribute(k_advance_flow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cache));
-  FL_CUDA(cudaDeviceSynchronize());  // k_init done
-  int rc0 = configure_flow(f, err);
-  if (rc0) return rc0;
-  const int ROUNDS = 16;
-  cudaGraph_t graph;
-  cudaGraphExec_t exec;
-  FL_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  int rc = GNUTS_OK;
-  for (int r = 0; r < ROUNDS && !rc; ++r) {
-    rc = launch_flow(f, m.dev, FM_GRAD, io, st, err);
-    if (!rc) k_advance_flow<<<blocks, threads, cache, st>>>(P, B, m.dev, flow_lp.p);
-  }
-  cudaError_t ce = cudaStreamEndCapture(st, &graph);
-  if (rc) return rc;
-  FL_CUDA(ce);
-  FL_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  struct GG { cudaGraph_t g; cudaGraphExec_t e; ~GG() { cudaGraphExecDestroy(e); cudaGraphDestroy(g); } } gg{graph, exec};
-  int* h_done = nullptr;
-  FL_CUDA(cudaMallocHost(&h_done, sizeof(int)));
-  struct HG { int* p; ~HG() { cudaFreeHost(p); } } hg{h_done};
-  cudaEvent_t e0, e1;
-  FL_CUDA(cudaEventCreate(&e0));
-  FL_CUDA(cudaEventCreate(&e1));
-  struct EG { cudaEvent_t a, b; ~EG() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{e0, e1};
-  const long long max_graphs = (long long)(per_chain_max / ROUNDS) + 16;
-  long long graphs = 0, rounds = 0;
-  // every 64th step runs one uncaptured round between events: the kernel durations
-  cudaEvent_t k0, k1, k2;
-  FL_CUDA(cudaEventCreate(&k0));
-  FL_CUDA(cudaEventCreate(&k1));
-  FL_CUDA(cudaEventCreate(&k2));
-  struct KG { cudaEvent_t a, b, c; ~KG() { cudaEventDestroy(a); cudaEventDestroy(b); cudaEventDestroy(c); } } kg{k0, k1, k2};
-  double fsum = 0, asum = 0;
-  int nt = 0;
-  FL_CUDA(cudaEventRecord(e0, st));
-  for (; graphs < max_graphs; ++graphs) {
-    const bool timed = (graphs & 63) == 5;
-    if (timed) {
-      FL_CUDA(cudaEventRecord(k0, st));
-      if ((rc = launch_flow(f, m.dev, FM_GRAD, io, st, err))) return rc;
-      FL_CUDA(cudaEventRecord(k1, st));
-      k_advance_flow<<<blocks, threads, cache, st>>>(P, B, m.dev, flow_lp.p);
-      FL_CUDA(cudaEventRecord(k2, st));
-      rounds += 1;
-    } else {
-      FL_CUDA(cudaGraphLaunch(exec, st));
-      rounds += ROUNDS;
-    }
-    FL_CUDA(cudaMemcpyAsync(h_done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost, st));
-    FL_CUDA(cudaStreamSynchronize(st));
-    if (timed && *h_done < P.C) {
-      float a = 0, b = 0;
-      if (cudaEventElapsedTime(&a, k0, k1) == cudaSuccess && cudaEventElapsedTime(&b, k1, k2) == cudaSuccess) {
-        fsum += a;
-        asum += b;
-        ++nt;
-      }
-    }
-    if (*h_done >= P.C) break;
-  }
-  FL_CUDA(cudaEventRecord(e1, st));
-  FL_CUDA(cudaEventSynchronize(e1));
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
-  stats[0] = (double)rounds;
-  stats[1] = ms;               // device ms
-  stats[2] = (double)rounds * 2;  // launches
-  stats[3] = nt ? 1e3 * fsum / nt : 0;  // flow kernel us
-  stats[4] = nt ? 1e3 * asum / nt : 0;  // state-machine kernel us
   return GNUTS_OK;
 }
 
@@ -1241,39 +1075,33 @@ int run_flow_fused(Model& m, const Flow& f, Params& P, const Bufs& B, double per
     return GNUTS_ERR_ARGUMENT;
   }
   const FlowDev F = dev_of(f);
-  // CTA shape: the largest T in {4, 2, 1} whose flow buffers plus (if they fit)
-  // the T chains' cached vectors stay within the shared-memory budget
+  // CTA shape: 8 warps (each contraction has at most 8 m-tiles, one per
+  // warp); T chains per CTA, the smallest power of two that keeps the grid
+  // within one CTA per SM, reduced while the flow region plus the chains'
+  // cached vectors exceed the shared-memory budget (the cache goes first)
+  int sms = 0, dev = 0;
+  FL_CUDA(cudaGetDevice(&dev));
+  FL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  int T = 1;
+  while (T < 8 && (P.C + T - 1) / T > sms) T <<= 1;
   const size_t chain_bytes = (size_t)P.cache_stride * sizeof(double);
-  int T = 0;
-  size_t flow_bytes = 0;
-  bool cache = false;
-  for (int t = 4; t >= 1 && !T; t >>= 1) {
-    FlowPlan pl = flow_plan(F, FLOW_SMEM_LIMIT);
-    if (pl.T == 0) break;
-    const size_t fb = pl.idx_bytes + 2 * pl.wbuf_bytes + (size_t)t * pl.warp_bytes;
-    if (fb + (size_t)t * chain_bytes <= FLOW_SMEM_LIMIT) {
-      T = t;
-      flow_bytes = fb;
-      cache = true;
-    } else if (t == 1 && fb <= FLOW_SMEM_LIMIT) {
-      T = 1;
-      flow_bytes = fb;
+  bool cache = true;
+  size_t flow_bytes = flow_tc_bytes(F, T);
+  while (flow_bytes + (cache ? (size_t)T * chain_bytes : 0) > FLOW_SMEM_LIMIT) {
+    if (cache) {
       cache = false;
+    } else if (T > 1) {
+      T >>= 1;
+      cache = true;
+      flow_bytes = flow_tc_bytes(F, T);
+    } else {
+      err = "flow does not fit in shared memory";
+      return GNUTS_ERR_ARGUMENT;
     }
   }
-  if (!T) {
-    err = "flow does not fit in shared memory";
-    return GNUTS_ERR_ARGUMENT;
-  }
   P.cache = cache ? 1 : 0;
-  const size_t smem = flow_align16(flow_bytes) + (cache ? (size_t)T * chain_bytes : 0);
-  flow_bytes = flow_align16(flow_bytes);
+  const size_t smem = flow_bytes + (cache ? (size_t)T * chain_bytes : 0);
   const int blocks = (P.C + T - 1) / T;
-  switch (f.H) {
-    case 128: FL_CUDA(cudaFuncSetAttribute(k_fused_flow<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); break;
-    case 64: FL_CUDA(cudaFuncSetAttribute(k_fused_flow<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); break;
-    default: FL_CUDA(cudaFuncSetAttribute(k_fused_flow<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); break;
-  }
   FL_CUDA(cudaDeviceSynchronize());  // k_init done
   int* h_done = nullptr;
   FL_CUDA(cudaMallocHost(&h_done, sizeof(int)));
@@ -1286,12 +1114,7 @@ int run_flow_fused(Model& m, const Flow& f, Params& P, const Bufs& B, double per
   long long launches = 0;
   FL_CUDA(cudaEventRecord(e0));
   for (; launches < max_launches; ++launches) {
-    switch (f.H) {
-      case 128: k_fused_flow<4><<<blocks, 32 * T, smem>>>(F, P, B, m.dev, flow_bytes); break;
-      case 64: k_fused_flow<2><<<blocks, 32 * T, smem>>>(F, P, B, m.dev, flow_bytes); break;
-      default: k_fused_flow<1><<<blocks, 32 * T, smem>>>(F, P, B, m.dev, flow_bytes); break;
-    }
-    FL_CUDA(cudaGetLastError());
+    FL_CUDA(flow_tc_fused_launch(m.dev.kind, F, P, B, m.dev, T, flow_bytes, blocks, smem));
     FL_CUDA(cudaMemcpy(h_done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
     if (*h_done >= P.C) {
       ++launches;

@@ -83,11 +83,13 @@ struct Flow {
   float clamp = 4.0f;
   std::vector<int> nb, na, idx, idx_off;  // idx: per layer b list then a list
   std::vector<long> th_off, w_off;        // th_off has L + 1 entries (th_off[L] = mu)
-  long th_rho = 0, n_params = 0, n_w16 = 0;
-  int stage_max = 0;
+  std::vector<long> wt_off;               // tensor-core weight blocks (zero-padded, see flow.cuh)
+  long th_rho = 0, n_params = 0, n_w16 = 0, n_w16t = 0;
+  int stage_max = 0, stage_max_tc = 0;
   int device = -1;
   float *theta = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
   uint16_t* w16 = nullptr;
+  uint16_t* w16t = nullptr;
   int* didx = nullptr;
   int* nvalid = nullptr;  // [2] valid-point counters of the training steps
   ~Flow();
@@ -127,6 +129,7 @@ int flow_log_prob_grad(Model& m, Flow& f, int n, const double* z, int jacobian, 
                        double* grad_theta, std::string& err);
 int flow_adam_step(Flow& f, const double* grad, int t, double lr, double b1, double b2, double eps,
                    std::string& err);
+int flow_log_prob_grad_tc(Model& m, Flow& f, int n, const double* z, double* lp, double* grad_z, std::string& err);
 int flow_train(Model& m, Flow& f, const gnuts_train_args& ta, double* loss_trace, std::string& err);
 // noalloc.cu: the allocation-free batched gradient (device pointers)
 int noalloc_log_prob_grad(const Model& m, int n, const double* q, int jac, double* lp, double* g, std::string& err);

@@ -171,6 +171,14 @@ int gnuts_flow_log_prob_grad(gnuts_model* m, gnuts_flow* f, int n, const double*
   return rc ? api_fail(rc, err) : GNUTS_OK;
 }
 
+int gnuts_flow_log_prob_grad_tc(gnuts_model* m, gnuts_flow* f, int n, const double* z, double* lp,
+                                double* grad_z) {
+  if (!m || !f || (n > 0 && (!z || !lp || !grad_z))) return api_fail(GNUTS_ERR_ARGUMENT, "null argument");
+  std::string err;
+  int rc = flow_log_prob_grad_tc(*Mo(m), *F(f), n, z, lp, grad_z, err);
+  return rc ? api_fail(rc, err) : GNUTS_OK;
+}
+
 int gnuts_flow_adam_step(gnuts_flow* f, const double* grad, int t, double lr, double beta1, double beta2,
                          double eps) {
   if (!f || !grad) return api_fail(GNUTS_ERR_ARGUMENT, "null argument");

@@ -827,4 +827,21 @@ struct Chain {
   }
 };
 
+// replay inputs of the transition-level entry point (chain ids, RNG offsets)
+struct ReplayBufs {
+  const unsigned* chain_ids;
+  const unsigned long long* rng_start;
+};
+
+// fused.cu / fused_kind.cu: the fused-mode kernel, one instantiation per
+// model kind (only that model's gradient is compiled into it)
+template <int KIND>
+cudaError_t fused_set_smem_k(int bytes);
+template <int KIND>
+cudaError_t fused_launch_k(int blocks, int threads, size_t smem, const Params& P, const Bufs& B, const DevModel& M,
+                           const ReplayBufs& RB);
+cudaError_t fused_set_smem(int kind, int bytes);
+cudaError_t fused_launch(int kind, int blocks, int threads, size_t smem, const Params& P, const Bufs& B,
+                         const DevModel& M, const ReplayBufs& RB);
+
 }  // namespace gnuts

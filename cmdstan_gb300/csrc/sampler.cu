@@ -32,10 +32,6 @@ namespace gnuts {
     }                                                                                        \
   } while (0)
 
-struct ReplayBufs {
-  const unsigned* chain_ids;
-  const unsigned long long* rng_start;
-};
 
 // ---------------------------------------------------------------- kernels
 __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, ReplayBufs RB) {
@@ -98,29 +94,6 @@ __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, R
     ch.Wg[d] = 0.0;
   }
   ch.init_candidate();
-  if (lane == 0) B.sc[warp] = s;
-}
-
-// Fused mode: the warp evaluates the gradient itself.
-__global__ void __launch_bounds__(128) k_fused(Params P, Bufs B, DevModel M, ReplayBufs RB) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= P.C) return;
-  Scal s = B.sc[warp];
-  if (s.phase >= PH_DONE) return;
-  const DevModel& Mc = chain_model(M, warp, P.C);
-  Chain ch(P, B, Mc, s, warp, lane);
-  if (RB.chain_ids) ch.chain_id = RB.chain_ids[warp];
-  extern __shared__ double gn_cache[];
-  if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
-  for (int b = 0; b < P.grad_budget; ++b) {
-    double lp = warp_log_prob_grad(Mc, ch.Wq, ch.Wg, 1, lane);
-    __syncwarp();
-    s.W_lp = lp;
-    if (!ch.advance()) break;
-  }
-  if (P.cache) ch.cache_detach();
-  __syncwarp();
   if (lane == 0) B.sc[warp] = s;
 }
 
@@ -573,8 +546,6 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                          uint64_t* counters, double* replay_q_out, gnuts_output* out,
                          gnuts_progress_fn progress, void* ctx, std::string& err);
 // flow.cu
-int run_flow_rounds(Model& m, const Flow& f, const Params& P, const Bufs& B, double per_chain_max, double* stats,
-                    std::string& err);
 int run_flow_fused(Model& m, const Flow& f, Params& P, const Bufs& B, double per_chain_max, double* stats,
                    std::string& err);
 int flow_finalize_draws(Model& m, const Flow& f, int rows, const double* zdraws, double* draws, int ncol,
@@ -641,14 +612,13 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     const bool rounds = use_rounds(m) && !p0 && !rc.flow;
     P.cache = bytes <= 160 * 1024 && !rounds;
     if (P.cache) {
-      GN_CUDA(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      GN_CUDA(fused_set_smem(m.dev.kind, (int)bytes));
       GN_CUDA(cudaFuncSetAttribute(k_advance, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     } else if (!rounds && (size_t)P.cache_stride * sizeof(double) <= 200 * 1024) {
       // large chains: the cache can still hold one or two chains per CTA
       // (the fused-mode autotuner decides whether that pays)
       const size_t one = (size_t)P.cache_stride * sizeof(double);
-      GN_CUDA(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)std::min<size_t>(2 * one <= 200 * 1024 ? 2 * one : one, 200 * 1024)));
+      GN_CUDA(fused_set_smem(m.dev.kind, (int)std::min<size_t>(2 * one <= 200 * 1024 ? 2 * one : one, 200 * 1024)));
     }
   }
 
@@ -776,8 +746,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
           const int bl = (C + w - 1) / w;
           const size_t sm = cch ? (size_t)w * P.cache_stride * sizeof(double) : 0;
           GN_CUDA(cudaEventRecord(t0));
-          k_fused<<<bl, 32 * w, sm>>>(Pt, B, m.dev, RB);
-          GN_CUDA(cudaGetLastError());
+          GN_CUDA(fused_launch(m.dev.kind, bl, 32 * w, sm, Pt, B, m.dev, RB));
           GN_CUDA(cudaEventRecord(t1));
           GN_CUDA(cudaEventSynchronize(t1));
           float ms = 0;
@@ -798,8 +767,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     const int fthreads = 32 * warps, fblocks = (C + warps - 1) / warps;
     const size_t fsmem = P.cache ? (size_t)warps * P.cache_stride * sizeof(double) : 0;
     for (long long l = 0; l < max_launches && done < C; ++l) {
-      k_fused<<<fblocks, fthreads, fsmem>>>(P, B, m.dev, RB);
-      GN_CUDA(cudaGetLastError());
+      GN_CUDA(fused_launch(m.dev.kind, fblocks, fthreads, fsmem, P, B, m.dev, RB));
       stats.rounds += 1;
       stats.launches += 1;
       GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));

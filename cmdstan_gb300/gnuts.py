@@ -34,7 +34,7 @@ EXPORTS = [
     "gnuts_version", "gnuts_summary", "gnuts_summary_columns", "gnuts_log_prob_grad_noalloc",
     "gnuts_flow_create", "gnuts_flow_destroy", "gnuts_flow_num_params", "gnuts_flow_set_params",
     "gnuts_flow_get_params", "gnuts_flow_init_affine", "gnuts_flow_forward", "gnuts_flow_inverse",
-    "gnuts_flow_log_prob_grad", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
+    "gnuts_flow_log_prob_grad", "gnuts_flow_log_prob_grad_tc", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
     "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt", "gnuts_train_args_default",
     "gnuts_summary_columns_gpu",
 ]
@@ -195,6 +195,7 @@ def load():
     lib.gnuts_flow_forward.argtypes = [vp, ip, dp, dp, dp]
     lib.gnuts_flow_inverse.argtypes = [vp, ip, dp, dp, dp]
     lib.gnuts_flow_log_prob_grad.argtypes = [vp, vp, ip, dp, ip, dp, dp, dp]
+    lib.gnuts_flow_log_prob_grad_tc.argtypes = [vp, vp, ip, dp, dp, dp]
     lib.gnuts_flow_adam_step.argtypes = [vp, dp, ip] + [ctypes.c_double] * 4
     lib.gnuts_train_args_default.argtypes = [ctypes.POINTER(TrainArgs)]
     lib.gnuts_train_args_default.restype = None
@@ -494,6 +495,14 @@ class Flow:
         _check(self._lib.gnuts_flow_log_prob_grad(model._h, self._h, n, _dp(z), int(bool(jacobian)), _dp(lp),
                                                   _dp(gz), _dp(gth)))
         return (lp, gz, gth) if param_grad else (lp, gz)
+
+    def log_prob_grad_tc(self, model, z):
+        """the sampler's tensor-core gradient pass at the rows of z (Jacobian on)"""
+        z = np.ascontiguousarray(np.atleast_2d(z), dtype=np.float64)
+        n = z.shape[0]
+        lp, gz = np.zeros(n), np.zeros_like(z)
+        _check(self._lib.gnuts_flow_log_prob_grad_tc(model._h, self._h, n, _dp(z), _dp(lp), _dp(gz)))
+        return lp, gz
 
     def adam_step(self, grad, t, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         g = np.ascontiguousarray(grad, dtype=np.float64)

@@ -246,6 +246,12 @@ int gnuts_flow_inverse(gnuts_flow* f, int n, const double* x, double* z, double*
  * gradient in theta (num_params) */
 int gnuts_flow_log_prob_grad(gnuts_model* m, gnuts_flow* f, int n, const double* z, int jacobian, double* lp,
                              double* grad_z, double* grad_theta);
+/* the sampler's gradient pass at n points: lp = lp_x(T(z)) + log|det|
+ * (jacobian on) and its gradient in z, from the tensor-core evaluation the
+ * learned sampler uses (BF16 weights, activations carried as three BF16
+ * parts, FP32 accumulation; the model at x in FP64) */
+int gnuts_flow_log_prob_grad_tc(gnuts_model* m, gnuts_flow* f, int n, const double* z, double* lp,
+                                double* grad_z);
 /* one Adam step (bias-corrected, step t >= 1) with the given gradient */
 int gnuts_flow_adam_step(gnuts_flow* f, const double* grad, int t, double lr, double beta1, double beta2,
                          double eps);

@@ -95,6 +95,32 @@ def test_log_prob_grad_matches_oracle(model_id):
     assert np.abs(gth - gsum).max() <= 3e-3 * np.abs(gsum).max()
 
 
+@pytest.mark.parametrize("model_id,hidden,n", [("funnel", 128, 37), ("hier", 128, 19), ("hier", 64, 5),
+                                               ("funnel", 32, 3)])
+def test_tensor_core_pass_matches_oracle(model_id, hidden, n):
+    """The sampler's gradient pass (mma.sync contractions on BF16 weights with
+    activations carried as three BF16 parts, FP32 accumulation) holds the
+    same tolerances as the FP32 SIMT pass: lp 1e-4 relative + 1e-3, gradient
+    3e-3 of its largest component; and it agrees with the SIMT pass."""
+    rng = np.random.default_rng(hidden + n)
+    data = workloads.funnel(100) if model_id == "funnel" else workloads.hier(seed=3)
+    m, om = gn.Model(model_id, data), oracle.OracleModel(model_id, data)
+    d = m.dim
+    of = oracle.OracleFlow(d, layers=8, hidden=hidden, clamp=4.0)
+    f = gn.Flow(d, layers=8, hidden=hidden, clamp=4.0)
+    th = _random_theta(of, rng, w2=0.03, rho=0.1)
+    f.set_params(th)
+    z = rng.normal(0, 0.7, (n, d)).astype(np.float32).astype(np.float64)
+    lp, gz = f.log_prob_grad_tc(m, z)
+    lps, gzs = f.log_prob_grad(m, z)
+    for i in range(n):
+        olp, ogz = of.log_prob_grad(om, th, z[i])
+        assert abs(lp[i] - olp) <= 1e-4 * abs(olp) + 1e-3, (i, lp[i], olp)
+        assert np.abs(gz[i] - ogz).max() <= 3e-3 * np.abs(ogz).max(), i
+    assert np.allclose(lp, lps, rtol=1e-5, atol=1e-3)
+    assert np.abs(gz - gzs).max() <= 1e-3 * np.abs(gzs).max()
+
+
 def test_adam_step_matches_oracle():
     rng = np.random.default_rng(5)
     of = oracle.OracleFlow(12, layers=4, hidden=32)

@@ -385,12 +385,35 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   RunConfig cfg{0, 0};
   cfg.flow = flow_ok ? fl : nullptr;
   cfg.stepsizes = flow_ok ? rf.eps.data() : rp.eps.data();
+  const double* final_minv = flow_ok ? rf.minv.data() : rp.minv.data();
+  std::vector<double> pooled_eps, pooled_minv;
+  if (flow_ok) {
+    // The pulled-back space is one shared coordinate system, so the kept
+    // flow sampler runs every chain with the chains' median adapted step size
+    // and elementwise median inverse metric.  A chain whose own adaptation
+    // collapsed in a poorly mapped region (tiny step, trees at max_depth)
+    // would otherwise set the wall time of the whole launch.
+    auto median = [](std::vector<double> v) {
+      std::sort(v.begin(), v.end());
+      const size_t n = v.size();
+      return n % 2 ? v[n / 2] : 0.5 * (v[n / 2 - 1] + v[n / 2]);
+    };
+    pooled_eps.assign(C, median(rf.eps));
+    pooled_minv.assign((size_t)C * D, 0.0);
+    std::vector<double> col(C);
+    for (int i = 0; i < D; ++i) {
+      for (int c = 0; c < C; ++c) col[c] = rf.minv[(size_t)c * D + i];
+      const double v = median(col);
+      for (int c = 0; c < C; ++c) pooled_minv[(size_t)c * D + i] = v;
+    }
+    cfg.stepsizes = pooled_eps.data();
+    final_minv = pooled_minv.data();
+  }
   std::vector<int64_t> nlf_fin(C, 0);
   int64_t* user_nlf = out ? out->n_leapfrog : nullptr;
   gnuts_output fin = out ? *out : gnuts_output{};
   if (!fin.n_leapfrog) fin.n_leapfrog = nlf_fin.data();
-  rc = run_nuts(m, afin, cfg, flow_ok ? z_flow.data() : q_plain.data(), flow_ok ? rf.minv.data() : rp.minv.data(),
-                &fin, progress, ctx, err);
+  rc = run_nuts(m, afin, cfg, flow_ok ? z_flow.data() : q_plain.data(), final_minv, &fin, progress, ctx, err);
   if (rc) return api_fail(rc, err);
   rep.final_seconds = now_s() - t0;
   for (int c = 0; c < C; ++c) rep.final_grads += fin.n_leapfrog[c];

@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "-I" + INC, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-I" + CSRC]
 
-CU_SOURCES = ["sampler.cu", "fused.cu", "grad_tc.cu", "noalloc.cu", "flow.cu", "summary_gpu.cu"]
+CU_SOURCES = ["sampler.cu", "fused.cu", "grad_tc.cu", "grad_wide.cu", "noalloc.cu", "flow.cu", "summary_gpu.cu"]
 # compiled once per model kind (-DGNUTS_KIND=k, k = 0..N_KINDS-1)
 CU_KIND_SOURCES = ["fused_kind.cu", "flow_tc_kind.cu"]
 N_KINDS = 7
@@ -101,7 +101,7 @@ def build(verbose=False, jobs=None):
                 print(out)
     so = os.path.join(LIB, "libgnuts.so")
     if _newer(so, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
+        _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart", "-lcublasLt"])
     cli_src = os.path.join(CLI, "gnuts_sample.cpp")
     exe = os.path.join(LIB, "gnuts-sample")
     cli_deps = [os.path.join(CLI, f) for f in os.listdir(CLI)] if os.path.isdir(CLI) else []

@@ -240,17 +240,45 @@ struct Chain {
       }
     }
   }
+  // The element loops below run in chunks of VCH elements per lane with every
+  // load of a chunk issued before its arithmetic and stores: the vectors live
+  // in global (or shared) memory behind pointers the compiler must assume may
+  // alias, so a plain loop makes each element a full memory round trip (63 of
+  // them per vector at D = 2003).  Each element's arithmetic and each lane's
+  // summation order are those of the plain loop.
   __device__ double dot(const double* a, const double* b) const {
     double t = 0;
-    for (int d = lane; d < D; d += 32) t += a[d] * b[d];
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double va[VCH], vb[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        va[j] = d < D ? a[d] : 0.0;
+        vb[j] = d < D ? b[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCH; ++j)
+        if (base + lane + 32 * j < D) t += va[j] * vb[j];
+    }
     return wsum(t);
   }
   // out = minv * p  (p must be visible to the whole warp for dense)
   __device__ void dtau(double* out, const double* p) const {
-    if (P.metric == 0) {
-      for (int d = lane; d < D; d += 32) out[d] = minv[d] * p[d];
-    } else if (P.metric == 2) {
-      for (int d = lane; d < D; d += 32) out[d] = p[d];
+    if (P.metric != 1) {
+      for (int base = 0; base < D; base += 32 * VCH) {
+        double vm[VCH], vp[VCH];
+#pragma unroll
+        for (int j = 0; j < VCH; ++j) {
+          const int d = base + lane + 32 * j;
+          vp[j] = d < D ? p[d] : 0.0;
+          vm[j] = d < D && P.metric == 0 ? minv[d] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < VCH; ++j) {
+          const int d = base + lane + 32 * j;
+          if (d < D) out[d] = P.metric == 0 ? vm[j] * vp[j] : vp[j];
+        }
+      }
     } else {
       __syncwarp();
       for (int d = lane; d < D; d += 32) {
@@ -291,17 +319,50 @@ struct Chain {
 
   // W.p += e/2 g ; W.q += e * minv W.p   (gradient at W.q then requested)
   __device__ void begin_leapfrog(double e) {
-    for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
     if (P.metric == 1) {
+      for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
       dtau(tmp, Wp);
       for (int d = lane; d < D; d += 32) Wq[d] += e * tmp[d];
     } else {
-      for (int d = lane; d < D; d += 32) Wq[d] += e * (P.metric == 0 ? minv[d] * Wp[d] : Wp[d]);
+      for (int base = 0; base < D; base += 32 * VCH) {
+        double vp[VCH], vg[VCH], vq[VCH], vm[VCH];
+#pragma unroll
+        for (int j = 0; j < VCH; ++j) {
+          const int d = base + lane + 32 * j;
+          const bool ok = d < D;
+          vp[j] = ok ? Wp[d] : 0.0;
+          vg[j] = ok ? Wg[d] : 0.0;
+          vq[j] = ok ? Wq[d] : 0.0;
+          vm[j] = ok && P.metric == 0 ? minv[d] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < VCH; ++j) {
+          const int d = base + lane + 32 * j;
+          if (d < D) {
+            const double pn = vp[j] + 0.5 * e * vg[j];
+            Wp[d] = pn;
+            Wq[d] = vq[j] + e * (P.metric == 0 ? vm[j] * pn : pn);
+          }
+        }
+      }
     }
     __syncwarp();
   }
   __device__ void complete_leapfrog(double e) {
-    for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double vp[VCH], vg[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        vp[j] = d < D ? Wp[d] : 0.0;
+        vg[j] = d < D ? Wg[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        if (d < D) Wp[d] = vp[j] + 0.5 * e * vg[j];
+      }
+    }
     ++s.n_grad;
     __syncwarp();
   }
@@ -429,11 +490,27 @@ struct Chain {
     dtau(Tsb, Wp);
     s.H0 = kinetic(Wp, Tsb) - s.W_lp;
     s.S_h = s.H0;
-    for (int d = lane; d < D; d += 32) {
-      double p = Wp[d];
-      Fq[d] = Wq[d]; Fp[d] = p; Fg[d] = Wg[d];
-      Bq[d] = Wq[d]; Bp[d] = p; Bg[d] = Wg[d];
-      Tpb[d] = p; Tpe[d] = p; Tse[d] = Tsb[d]; Trho[d] = p;
+    for (int base = 0; base < D; base += 32 * VCH) {
+      double vp[VCH], vq[VCH], vg[VCH], vs[VCH];
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        const bool ok = d < D;
+        vp[j] = ok ? Wp[d] : 0.0;
+        vq[j] = ok ? Wq[d] : 0.0;
+        vg[j] = ok ? Wg[d] : 0.0;
+        vs[j] = ok ? Tsb[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCH; ++j) {
+        const int d = base + lane + 32 * j;
+        if (d < D) {
+          const double p = vp[j];
+          Fq[d] = vq[j]; Fp[d] = p; Fg[d] = vg[j];
+          Bq[d] = vq[j]; Bp[d] = p; Bg[d] = vg[j];
+          Tpb[d] = p; Tpe[d] = p; Tse[d] = vs[j]; Trho[d] = p;
+        }
+      }
     }
     s.F_lp = s.W_lp;
     s.B_lp = s.W_lp;
@@ -541,22 +618,42 @@ struct Chain {
     if (P.metric == 1) {
       dtau(tmp, Wp);
       for (int d = lane; d < D; d += 32) kin += Wp[d] * tmp[d];
-    } else {
       for (int d = lane; d < D; d += 32) {
         const double p = Wp[d];
-        kin += p * (P.metric == 0 ? minv[d] * p : p);
+        const double ps = tmp[d];
+        pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
+        rq[d] = Wq[d]; rg[d] = Wg[d];
+      }
+    } else {
+      // the leaf's kinetic energy and its record in one chunked pass
+      for (int base = 0; base < D; base += 32 * VCH) {
+        double vp[VCH], vm[VCH], vq[VCH], vg[VCH];
+#pragma unroll
+        for (int j = 0; j < VCH; ++j) {
+          const int d = base + lane + 32 * j;
+          const bool ok = d < D;
+          vp[j] = ok ? Wp[d] : 0.0;
+          vm[j] = ok && P.metric == 0 ? minv[d] : 0.0;
+          vq[j] = ok ? Wq[d] : 0.0;
+          vg[j] = ok ? Wg[d] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < VCH; ++j) {
+          const int d = base + lane + 32 * j;
+          if (d < D) {
+            const double p = vp[j];
+            const double ps = P.metric == 0 ? vm[j] * p : p;
+            kin += p * ps;
+            pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
+            rq[d] = vq[j]; rg[d] = vg[j];
+          }
+        }
       }
     }
     double h = 0.5 * wsum(kin) - s.W_lp;
     if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
     if (h - s.H0 > 1000.0) s.divergent = 1;
     s.sum_metro += (s.H0 - h > 0) ? 1.0 : exp(s.H0 - h);
-    for (int d = lane; d < D; d += 32) {
-      const double p = Wp[d];
-      const double ps = P.metric == 1 ? tmp[d] : (P.metric == 0 ? minv[d] * p : p);
-      pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
-      rq[d] = Wq[d]; rg[d] = Wg[d];
-    }
     rlsw(r) = s.H0 - h;
     rlp(r) = s.W_lp;
     rh(r) = h;

@@ -20,6 +20,7 @@
 #include "nuts_device.cuh"
 #include "batched.cuh"
 #include "grad_tc.h"
+#include "grad_wide.h"
 
 namespace gnuts {
 
@@ -360,7 +361,11 @@ struct GradSetup {
   Arena ar;
   GradOut G{};
   TcPlan* plan = nullptr;
-  ~GradSetup() { tc_destroy(plan); }
+  WidePlan* wide = nullptr;
+  ~GradSetup() {
+    tc_destroy(plan);
+    wide_destroy(wide);
+  }
 };
 
 int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* done_count, std::string& err) {
@@ -376,6 +381,15 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
     if (st) return st;
     G.tc = gs.plan;
     G.Cpad = (C + 127) / 128 * 128;
+    return GNUTS_OK;
+  }
+  if (prec == GNUTS_PRECISION_MIXED && wide_supported(M)) {
+    // wider than the tcgen05 tile: cuBLASLt GEMMs around this project's epilogue
+    int st = wide_create(M, C, &gs.wide, &G.coef64, &G.part_lp, &G.part_g, err);
+    if (st) return st;
+    G.wide = gs.wide;
+    G.S = 1;
+    G.rows_per_split = M.N;
     return GNUTS_OK;
   }
   // row splits: enough CTAs to fill 152 SMs a few times over
@@ -399,6 +413,8 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
 void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
   if (G.tc) {
     tc_launch((const TcPlan*)G.tc, st);
+  } else if (G.wide) {
+    wide_launch((const WidePlan*)G.wide, G, M, st);
   } else {
     dim3 grid((G.C + GLM_CT - 1) / GLM_CT, G.S);
     const bool small = M.K <= GLM_KC;

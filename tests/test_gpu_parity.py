@@ -344,6 +344,42 @@ def test_tensor_core_gradient_close_to_fp64(N, D, n):
     assert np.max(np.abs(g[0] - og)) <= 3e-3 * np.max(np.abs(og))
 
 
+@pytest.mark.parametrize("mid,data", [
+    ("horseshoe", workloads.horseshoe(seed=11, N=8192, D=256, n_nonzero=6)),
+    ("logistic", workloads.logistic(seed=12, N=8192, D=136)),
+], ids=["horseshoe_256", "logistic_136"])
+def test_wide_gradient_close_to_fp64(mid, data):
+    """Designs wider than the tcgen05 tile go through cuBLASLt BF16 GEMMs
+    (coefficients split hi/lo, residuals BF16, FP32 accumulation) around the
+    project's epilogue kernel.  Same tolerances as the tcgen05 path: lp
+    relative 1e-4, gradient 2e-3 of its largest component; the FP64 path of
+    the same points stays at 1e-10."""
+    gm, om = _pair(mid, data)
+    rng = np.random.default_rng(17)
+    q = rng.normal(0, 0.3, (9, gm.dim))
+    lp, g = gm.log_prob_grad(q, precision=gn.PRECISION_MIXED)
+    lp64, g64 = gm.log_prob_grad(q)
+    for i in range(q.shape[0]):
+        olp, og = om.log_prob_grad(q[i])
+        assert abs(lp[i] - olp) <= 1e-4 * abs(olp), (i, lp[i], olp)
+        assert np.max(np.abs(g[i] - og)) <= 2e-3 * np.max(np.abs(og)), (i, np.max(np.abs(g[i] - og)))
+        assert abs(lp64[i] - olp) <= 1e-10 * abs(olp)
+
+
+def test_wide_sampler_moments_match_oracle():
+    """NUTS on the cuBLASLt wide-design gradient: moments agree with the
+    FP64 oracle's chains within 4.5 combined MCSE."""
+    data = workloads.logistic(seed=22, N=8192, D=136)
+    gm, om = _pair("logistic", data)
+    fit = gm.sample(num_chains=64, seed=5, precision=gn.PRECISION_MIXED, num_warmup=300, num_samples=300)
+    od, _, _, _ = om.run_chains(16, threads=16, seed=5, num_warmup=300, num_samples=300)
+    for j in range(0, gm.num_constrained, 7):
+        x, y = fit.draws[:, :, 7 + j], od[:, :, 7 + j]
+        sx, sy = oracle.summary(x), oracle.summary(y)
+        assert sx["rhat"] < 1.02
+        assert abs(sx["mean"] - sy["mean"]) < 4.5 * np.hypot(sx["mcse"], sy["mcse"]), gm.param_names[j]
+
+
 def test_tensor_core_sampler_moments_match_oracle():
     data = workloads.logistic(seed=21, N=6000, D=10)
     gm, om = _pair("logistic", data)

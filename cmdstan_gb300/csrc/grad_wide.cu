@@ -17,7 +17,8 @@
 // coefficient transforms and priors stay in stage_request / reduce_gradient.
 // Precision matches the tcgen05 path: X BF16-exact, coefficients split into
 // two BF16 parts (16 significant bits), FP32 accumulation, residuals BF16,
-// per-block sums in FP64 summed in a fixed order (bitwise reproducible).
+// per-warp sums in FP32 and per-block / per-chain sums in FP64, all in a
+// fixed order (bitwise reproducible run to run).
 #include <cublasLt.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -69,7 +70,10 @@ __global__ void k_wide_stage(const double* coef64, int C, int K, __nv_bfloat16* 
 }
 
 // eta, the likelihood's lp terms and residuals of chain blockIdx.y over rows
-// [blockIdx.x * WE_ROWS, +WE_ROWS); FP32 per element, block sums in FP64
+// [blockIdx.x * WE_ROWS, +WE_ROWS).  FP32 per element and per warp (shuffle
+// sums in a fixed order); the block's eight warp sums are added in FP64 by
+// one thread: the block does two FP64 additions per warp, not a tree of them
+// (this part's FP64 pipe is narrow).
 __global__ void __launch_bounds__(WE_THREADS) k_wide_epi(const float* __restrict__ h, const double* coef64,
                                                          const int* __restrict__ y, int N, int C, int K,
                                                          __nv_bfloat16* __restrict__ r, double* plp,
@@ -81,58 +85,77 @@ __global__ void __launch_bounds__(WE_THREADS) k_wide_epi(const float* __restrict
   __nv_bfloat16* rr = r + (size_t)c * N;
   float lp = 0.f, rs = 0.f;
   const int n0 = blockIdx.x * WE_ROWS + threadIdx.x;
+  float eh[4], el[4], yv[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int n = n0 + j * WE_THREADS;
+    const bool ok = n < N;
+    eh[j] = ok ? hh[n] : 0.f;
+    el[j] = ok ? hl[n] : 0.f;
+    yv[j] = ok ? (float)y[n] : 0.f;
+  }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int n = n0 + j * WE_THREADS;
     if (n < N) {
-      const float eta = hh[n] + hl[n] + b0;
-      const float yv = (float)y[n];
+      const float eta = eh[j] + el[j] + b0;
       // softplus(eta) = max(eta, 0) + log1p(exp(-|eta|)); inv_logit from the same exponential
       const float e = __expf(-fabsf(eta));
       const float d = 1.f + e;
       const float sp = fmaxf(eta, 0.f) + __logf(d);
-      const float sig = (eta >= 0.f ? 1.f : e) / d;
-      lp += fmaf(yv, eta, -sp);
-      const float res = yv - sig;
+      const float sig = __fdividef(eta >= 0.f ? 1.f : e, d);
+      lp += fmaf(yv[j], eta, -sp);
+      const float res = yv[j] - sig;
       rs += res;
       rr[n] = __float2bfloat16_rn(res);
     }
   }
-  __shared__ double s_lp[WE_THREADS], s_r[WE_THREADS];
-  s_lp[threadIdx.x] = (double)lp;
-  s_r[threadIdx.x] = (double)rs;
-  __syncthreads();
-  for (int o = WE_THREADS / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      s_lp[threadIdx.x] += s_lp[threadIdx.x + o];
-      s_r[threadIdx.x] += s_r[threadIdx.x + o];
-    }
-    __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lp += __shfl_xor_sync(0xffffffffu, lp, o);
+    rs += __shfl_xor_sync(0xffffffffu, rs, o);
   }
+  __shared__ float s_lp[WE_THREADS / 32], s_r[WE_THREADS / 32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    s_lp[w] = lp;
+    s_r[w] = rs;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    plp[(size_t)blockIdx.x * C + c] = s_lp[0];
-    pr[(size_t)blockIdx.x * C + c] = s_r[0];
+    double a = 0, b = 0;
+    for (int k = 0; k < WE_THREADS / 32; ++k) {
+      a += (double)s_lp[k];
+      b += (double)s_r[k];
+    }
+    plp[(size_t)blockIdx.x * C + c] = a;
+    pr[(size_t)blockIdx.x * C + c] = b;
   }
 }
 
-// block sums (fixed order) and GEMM2's columns -> the consumer's partials
+// block sums and GEMM2's columns -> the consumer's partials.  One warp per
+// chain: lane l sums blocks l, l + 32, ... in order, then a fixed butterfly.
 __global__ void k_wide_final(const double* plp, const double* pr, const float* gk, int NB, int C, int K,
                              double* part_lp, double* part_g) {
-  const size_t n = (size_t)C * (K + 1);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i / (K + 1)), k = (int)(i % (K + 1));
-    if (k == 0) {
-      double a = 0, b = 0;
-      for (int s = 0; s < NB; ++s) {
-        a += plp[(size_t)s * C + c];
-        b += pr[(size_t)s * C + c];
-      }
-      part_lp[c] = a;
-      part_g[i] = b;
-    } else {
-      part_g[i] = (double)gk[(size_t)c * K + (k - 1)];
-    }
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (c >= C) return;
+  double a = 0, b = 0;
+  for (int s = lane; s < NB; s += 32) {
+    a += plp[(size_t)s * C + c];
+    b += pr[(size_t)s * C + c];
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  double* g = part_g + (size_t)c * (K + 1);
+  if (lane == 0) {
+    part_lp[c] = a;
+    g[0] = b;
+  }
+  const float* src = gk + (size_t)c * K;
+  for (int k = lane; k < K; k += 32) g[1 + k] = (double)src[k];
 }
 
 namespace {
@@ -256,8 +279,7 @@ int wide_launch(const WidePlan* p, const GradOut& G, const DevModel& M, cudaStre
   if (cublasLtMatmul(p->lt, p->d2, &one, M.Xb, p->a2, p->r, p->b2, &zero, p->gk, p->c2, p->gk, p->c2, &p->algo2,
                      p->ws, WIDE_WS_BYTES, st) != CUBLAS_STATUS_SUCCESS)
     return GNUTS_ERR_CUDA;
-  k_wide_final<<<std::min(4096, (int)(((size_t)C * (K + 1) + 255) / 256)), 256, 0, st>>>(
-      p->plp, p->pr, p->gk, p->NB, C, K, G.part_lp, G.part_g);
+  k_wide_final<<<(C * 32 + 255) / 256, 256, 0, st>>>(p->plp, p->pr, p->gk, p->NB, C, K, G.part_lp, G.part_g);
   return cudaGetLastError() == cudaSuccess ? GNUTS_OK : GNUTS_ERR_CUDA;
 }
 

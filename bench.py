@@ -405,8 +405,10 @@ def main():
     kw = dict(num_chains=N_CHAINS, num_warmup=NUM_WARMUP, num_samples=NUM_SAMPLES, refresh=0,
               precision=gn.PRECISION_MIXED)
 
+    from cmdstan_gb300.replicas import chain_id_base, reduce_job
+
     def one_step(seed):
-        return model.sample(seed=seed, chain_id=1 + rank * N_CHAINS, **kw)
+        return model.sample(seed=seed, chain_id=chain_id_base(rank, N_CHAINS), **kw)
 
     for i in range(args.warmup):
         one_step(1000 + i)
@@ -431,15 +433,7 @@ def main():
     # whole-job throughput: leapfrogs over the sampler's device time (max over ranks)
     lf = float(sum(f.n_leapfrog.sum() for f in fits))
     dev_ms = float(sum(f.timing["device_ms"] for f in fits))
-    if dist:
-        t = torch.tensor([lf, dev_ms, sum(times)], dtype=torch.float64, device="cuda")
-        tot = t.clone()
-        dist.all_reduce(tot[:1])
-        mx = t[1:].clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        lf, dev_ms, wall_ms = float(tot[0]), float(mx[0]), float(mx[1])
-    else:
-        wall_ms = float(sum(times))
+    lf, dev_ms, wall_ms = reduce_job(lf, dev_ms, float(sum(times)), dist, device="cuda")
     value = lf / (dev_ms / 1e3)
     # ESS / R-hat of the last run
     last = fits[-1]
@@ -467,7 +461,7 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         m2 = gn.Model("logistic", data)
-        f2 = m2.sample(seed=100 + i, chain_id=1 + rank * N_CHAINS, **kw)
+        f2 = m2.sample(seed=100 + i, chain_id=chain_id_base(rank, N_CHAINS), **kw)
         del m2
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)

@@ -106,7 +106,8 @@ def build(verbose=False, jobs=None):
     exe = os.path.join(LIB, "gnuts-sample")
     cli_deps = [os.path.join(CLI, f) for f in os.listdir(CLI)] if os.path.isdir(CLI) else []
     if os.path.exists(cli_src) and _newer(exe, cli_deps + [so, os.path.join(INC, "gnuts.h")]):
-        _run(["g++"] + CXX_FLAGS + ["-I" + CLI, cli_src, "-o", exe, "-L" + LIB, "-lgnuts", "-Wl,-rpath,$ORIGIN"])
+        _run(["g++"] + CXX_FLAGS + ["-pthread", "-I" + CLI, cli_src, "-o", exe, "-L" + LIB, "-lgnuts",
+                                    "-Wl,-rpath,$ORIGIN"])
     return so
 
 

@@ -25,6 +25,9 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <algorithm>
+#include <atomic>
+#include <thread>
 #include <vector>
 
 #include "arg_tree.hpp"
@@ -603,9 +606,16 @@ int main(int argc, char** argv) {
     const auto csv_names = make_filenames(output_file, "", ".csv", num_chains, id);
     const int n_warm_saved = save_warmup ? (num_warmup + thin - 1) / thin : 0;
     const std::string datetime = utc_now();
-    for (int c = 0; c < num_chains; ++c) {
+    // one file per chain (file.hpp:189-212), formatted on all host cores:
+    // chains are claimed from an atomic counter; the console lines and the
+    // first error are reported in chain order afterwards
+    std::vector<std::string> chain_msg(num_chains), chain_err(num_chains);
+    auto write_chain = [&](int c) {
       std::ofstream f(csv_names[c]);
-      if (!f) throw std::runtime_error("Can't open output file " + csv_names[c]);
+      if (!f) {
+        chain_err[c] = "Can't open output file " + csv_names[c];
+        return;
+      }
       f << "# stan_version_major = 2\n# stan_version_minor = 36\n# stan_version_patch = 0\n";
       f << "# model = " << model_name << "\n# start_datetime = " << datetime << "\n";
       for (auto& l : cfg_lines) f << "# " << l << "\n";
@@ -650,10 +660,29 @@ int main(int argc, char** argv) {
       f << "# \n#  Elapsed Time: " << fmt(w, 6) << " seconds (Warm-up)\n";
       f << "#                " << fmt(s, 6) << " seconds (Sampling)\n";
       f << "#                " << fmt(w + s, 6) << " seconds (Total)\n# \n";
-      if (!f) throw std::runtime_error("error writing " + csv_names[c]);
-      std::cout << (num_chains > 1 ? "Chain [" + std::to_string(id + (unsigned)c) + "] " : std::string())
-                << "Elapsed Time: " << fmt(w, 6) << " seconds (Warm-up), " << fmt(s, 6) << " seconds (Sampling), "
-                << fmt(w + s, 6) << " seconds (Total)" << std::endl;
+      if (!f) {
+        chain_err[c] = "error writing " + csv_names[c];
+        return;
+      }
+      chain_msg[c] = (num_chains > 1 ? "Chain [" + std::to_string(id + (unsigned)c) + "] " : std::string()) +
+                     "Elapsed Time: " + fmt(w, 6) + " seconds (Warm-up), " + fmt(s, 6) + " seconds (Sampling), " +
+                     fmt(w + s, 6) + " seconds (Total)";
+    };
+    {
+      const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+      const int nt = std::min(hw, num_chains);
+      std::atomic<int> next{0};
+      auto worker = [&]() {
+        for (int c = next++; c < num_chains; c = next++) write_chain(c);
+      };
+      std::vector<std::thread> pool;
+      for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+      worker();
+      for (auto& t : pool) t.join();
+    }
+    for (int c = 0; c < num_chains; ++c) {
+      if (!chain_err[c].empty()) throw std::runtime_error(chain_err[c]);
+      std::cout << chain_msg[c] << std::endl;
     }
 
     // ---- adapted metric as JSON (command.hpp:247-261)

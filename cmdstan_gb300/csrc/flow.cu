@@ -1,6 +1,8 @@
 // Affine-coupling flow kernels (forward, inverse, log-determinant, adjoint,
-// parameter gradient, Adam) and the NUTS round driver in the pulled-back
-// space.  The map and the parameter layout are described in flow.cuh.
+// parameter gradient, Adam), reverse-KL training, and the host side of the
+// fused NUTS sampler in the pulled-back space (its kernels, on the tensor
+// cores, are in flow_tc_kind.cu).  The map and the layouts are described in
+// flow.cuh.
 //
 // No counterpart in the reference: CmdStan's NUTS (reached through
 // stan::services::sample::hmc_nuts_diag_e_adapt, src/cmdstan/command.hpp:

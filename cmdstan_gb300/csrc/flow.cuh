@@ -23,7 +23,8 @@
 // forward stage streams [W2 | W1] and an adjoint stage [W1 | W2^T], each one
 // contiguous range.
 //
-// Execution: one warp per point, FLOW_T points per CTA.  The CTA streams one
+// Execution of the SIMT kernels (training, the public forward / log-density
+// entry points): one warp per point, up to 4 points per CTA.  The CTA streams one
 // layer's BF16 weights at a time into shared memory with cp.async (double
 // buffered: the next stage's copy is in flight while this stage computes),
 // so every warp of the CTA reads them on chip.  Lane l owns hidden units

@@ -68,8 +68,11 @@ struct Params {
 // vectors cached per chain (diag / unit metric also caches minv, wm, wm2)
 constexpr int NCACHE_VEC = 17;
 constexpr int NCACHE_VEC_DIAG = 20;
-// elements per lane whose loads are issued together in the record loops
+// elements per lane whose loads are issued together: VCH in the record
+// loops (merge, finish_doubling: nine or ten vectors), VCW in the loops over
+// at most four vectors (leapfrog, leaf record, dot, metric product, copies)
 constexpr int VCH = 4;
+constexpr int VCW = 8;
 
 struct Bufs {
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg;
@@ -204,34 +207,34 @@ struct Chain {
   }
 
   // ---------------- vector helpers ----------------
-  // chunks of 4 elements per lane: every load of a chunk is issued before its
-  // stores, so a copy costs one memory round trip per 128 elements
+  // chunks of VCW elements per lane: every load of a chunk is issued before
+  // its stores, so a copy costs one memory round trip per 32 VCW elements
   __device__ void copy(double* dst, const double* src) const {
-    for (int base = 0; base < D; base += 32 * VCH) {
-      double v[VCH];
+    for (int base = 0; base < D; base += 32 * VCW) {
+      double v[VCW];
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         v[j] = d < D ? src[d] : 0.0;
       }
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         if (d < D) dst[d] = v[j];
       }
     }
   }
   __device__ void copy2(double* d1, const double* s1, double* d2, const double* s2) const {
-    for (int base = 0; base < D; base += 32 * VCH) {
-      double v[VCH], w[VCH];
+    for (int base = 0; base < D; base += 32 * VCW) {
+      double v[VCW], w[VCW];
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         v[j] = d < D ? s1[d] : 0.0;
         w[j] = d < D ? s2[d] : 0.0;
       }
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         if (d < D) {
           d1[d] = v[j];
@@ -240,7 +243,7 @@ struct Chain {
       }
     }
   }
-  // The element loops below run in chunks of VCH elements per lane with every
+  // The element loops below run in chunks of VCW elements per lane with every
   // load of a chunk issued before its arithmetic and stores: the vectors live
   // in global (or shared) memory behind pointers the compiler must assume may
   // alias, so a plain loop makes each element a full memory round trip (63 of
@@ -248,16 +251,16 @@ struct Chain {
   // summation order are those of the plain loop.
   __device__ double dot(const double* a, const double* b) const {
     double t = 0;
-    for (int base = 0; base < D; base += 32 * VCH) {
-      double va[VCH], vb[VCH];
+    for (int base = 0; base < D; base += 32 * VCW) {
+      double va[VCW], vb[VCW];
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         va[j] = d < D ? a[d] : 0.0;
         vb[j] = d < D ? b[d] : 0.0;
       }
 #pragma unroll
-      for (int j = 0; j < VCH; ++j)
+      for (int j = 0; j < VCW; ++j)
         if (base + lane + 32 * j < D) t += va[j] * vb[j];
     }
     return wsum(t);
@@ -265,16 +268,16 @@ struct Chain {
   // out = minv * p  (p must be visible to the whole warp for dense)
   __device__ void dtau(double* out, const double* p) const {
     if (P.metric != 1) {
-      for (int base = 0; base < D; base += 32 * VCH) {
-        double vm[VCH], vp[VCH];
+      for (int base = 0; base < D; base += 32 * VCW) {
+        double vm[VCW], vp[VCW];
 #pragma unroll
-        for (int j = 0; j < VCH; ++j) {
+        for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           vp[j] = d < D ? p[d] : 0.0;
           vm[j] = d < D && P.metric == 0 ? minv[d] : 0.0;
         }
 #pragma unroll
-        for (int j = 0; j < VCH; ++j) {
+        for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           if (d < D) out[d] = P.metric == 0 ? vm[j] * vp[j] : vp[j];
         }
@@ -324,10 +327,10 @@ struct Chain {
       dtau(tmp, Wp);
       for (int d = lane; d < D; d += 32) Wq[d] += e * tmp[d];
     } else {
-      for (int base = 0; base < D; base += 32 * VCH) {
-        double vp[VCH], vg[VCH], vq[VCH], vm[VCH];
+      for (int base = 0; base < D; base += 32 * VCW) {
+        double vp[VCW], vg[VCW], vq[VCW], vm[VCW];
 #pragma unroll
-        for (int j = 0; j < VCH; ++j) {
+        for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           const bool ok = d < D;
           vp[j] = ok ? Wp[d] : 0.0;
@@ -336,7 +339,7 @@ struct Chain {
           vm[j] = ok && P.metric == 0 ? minv[d] : 0.0;
         }
 #pragma unroll
-        for (int j = 0; j < VCH; ++j) {
+        for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           if (d < D) {
             const double pn = vp[j] + 0.5 * e * vg[j];
@@ -349,16 +352,16 @@ struct Chain {
     __syncwarp();
   }
   __device__ void complete_leapfrog(double e) {
-    for (int base = 0; base < D; base += 32 * VCH) {
-      double vp[VCH], vg[VCH];
+    for (int base = 0; base < D; base += 32 * VCW) {
+      double vp[VCW], vg[VCW];
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         vp[j] = d < D ? Wp[d] : 0.0;
         vg[j] = d < D ? Wg[d] : 0.0;
       }
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         if (d < D) Wp[d] = vp[j] + 0.5 * e * vg[j];
       }
@@ -490,10 +493,10 @@ struct Chain {
     dtau(Tsb, Wp);
     s.H0 = kinetic(Wp, Tsb) - s.W_lp;
     s.S_h = s.H0;
-    for (int base = 0; base < D; base += 32 * VCH) {
-      double vp[VCH], vq[VCH], vg[VCH], vs[VCH];
+    for (int base = 0; base < D; base += 32 * VCW) {
+      double vp[VCW], vq[VCW], vg[VCW], vs[VCW];
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         const bool ok = d < D;
         vp[j] = ok ? Wp[d] : 0.0;
@@ -502,7 +505,7 @@ struct Chain {
         vs[j] = ok ? Tsb[d] : 0.0;
       }
 #pragma unroll
-      for (int j = 0; j < VCH; ++j) {
+      for (int j = 0; j < VCW; ++j) {
         const int d = base + lane + 32 * j;
         if (d < D) {
           const double p = vp[j];
@@ -626,10 +629,10 @@ struct Chain {
       }
     } else {
       // the leaf's kinetic energy and its record in one chunked pass
-      for (int base = 0; base < D; base += 32 * VCH) {
-        double vp[VCH], vm[VCH], vq[VCH], vg[VCH];
+      for (int base = 0; base < D; base += 32 * VCW) {
+        double vp[VCW], vm[VCW], vq[VCW], vg[VCW];
 #pragma unroll
-        for (int j = 0; j < VCH; ++j) {
+        for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           const bool ok = d < D;
           vp[j] = ok ? Wp[d] : 0.0;
@@ -638,7 +641,7 @@ struct Chain {
           vg[j] = ok ? Wg[d] : 0.0;
         }
 #pragma unroll
-        for (int j = 0; j < VCH; ++j) {
+        for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           if (d < D) {
             const double p = vp[j];

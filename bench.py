@@ -153,6 +153,7 @@ def cpu_sample(data, seconds=15.0, threads=None):
     _, _, _, ng = om.run_chains(threads, threads=threads, inits=w, inv_metric=var, num_samples=iters, **kw)
     wall = time.time() - t
     return {"value": float(ng.sum() / wall), "unit": "grad-evals/s", "cores": threads, "kind": "port",
+            "wall_s": wall,
             "sample": "%d chains x %d transitions (adaptation off, started at the posterior mode, Laplace diag "
                       "metric, step 0.7) of the same workload, FP64, %d host threads; %.1f s" %
                       (threads, iters, threads, wall)}
@@ -170,14 +171,16 @@ def run_reference(args):
             res.append(r)
     v = float(np.mean([r["value"] for r in res]))
     line = {"metric": METRIC, "value": v, "unit": "grad-evals/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean([r["wall_s"] for r in res])) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
             "config": config(args),
             "cpu_baseline": {"value": v, "unit": "grad-evals/s", "cores": res[-1]["cores"], "kind": "port",
                              "sample": res[-1]["sample"]},
             "e2e": {"value": v, "unit": "grad-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's own implementation (stan submodule) is absent from the reference tree; "
-                    "the CPU oracle restating it times the CPU path"}
+                    "the CPU oracle restating it times the CPU path; a step is one bounded sample of the "
+                    "workload (ms_per_step is its wall time)"}
     print(json.dumps(line))
 
 

@@ -408,13 +408,15 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   return GNUTS_OK;
 }
 
-// the batched contraction (tensor-core or SIMT); its row-split partials are
-// summed by the consumer (reduce_gradient, inside the state-machine kernel)
-void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
+// the batched contraction (tcgen05, cuBLASLt wide-design or SIMT); its
+// partials are summed by the consumer (reduce_gradient, inside the
+// state-machine kernel).  Returns the cuBLASLt path's enqueue status; the
+// kernel paths report through the stream's launch errors.
+int launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
   if (G.tc) {
     tc_launch((const TcPlan*)G.tc, st);
   } else if (G.wide) {
-    wide_launch((const WidePlan*)G.wide, G, M, st);
+    return wide_launch((const WidePlan*)G.wide, G, M, st);
   } else {
     dim3 grid((G.C + GLM_CT - 1) / GLM_CT, G.S);
     const bool small = M.K <= GLM_KC;
@@ -426,6 +428,7 @@ void launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
       else k_glm_simt<float, 8><<<grid, GLM_THREADS, 0, st>>>(G, M);
     }
   }
+  return GNUTS_OK;
 }
 
 }  // namespace
@@ -438,7 +441,10 @@ int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, d
   if (st) return st;
   const int threads = 128, blocks = (n * 32 + threads - 1) / threads;
   k_stage_points<<<blocks, threads>>>(gs.G, M, n, dq);
-  launch_glm(gs.G, M, 0);
+  if (launch_glm(gs.G, M, 0)) {
+    err = "the batched gradient's GEMM could not be launched";
+    return GNUTS_ERR_CUDA;
+  }
   k_reduce_points<<<blocks, threads>>>(gs.G, M, n, dq, jac, dl, dg);
   GN_CUDA(cudaGetLastError());
   GN_CUDA(cudaDeviceSynchronize());
@@ -475,11 +481,17 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   GN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  int glm_rc = GNUTS_OK;
   for (int r = 0; r < ROUNDS; ++r) {
-    launch_glm(G, M, stream);
+    glm_rc |= launch_glm(G, M, stream);
     k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
   }
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
+  if (glm_rc) {
+    cudaGraphDestroy(graph);
+    err = "the batched gradient's GEMM could not be captured";
+    return GNUTS_ERR_CUDA;
+  }
   GN_CUDA(cudaEventRecord(tev[3], stream));
   GN_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   struct GraphGuard { cudaGraph_t g; cudaGraphExec_t e; ~GraphGuard() { cudaGraphExecDestroy(e); cudaGraphDestroy(g); } } gg{graph, exec};
@@ -501,7 +513,10 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
     const bool timed = (l & 63) == 5;
     if (timed) {
       GN_CUDA(cudaEventRecord(tev[0], stream));
-      launch_glm(G, M, stream);
+      if (launch_glm(G, M, stream)) {
+        err = "the batched gradient's GEMM could not be launched";
+        return GNUTS_ERR_CUDA;
+      }
       GN_CUDA(cudaEventRecord(tev[1], stream));
       k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
       GN_CUDA(cudaEventRecord(tev[2], stream));

@@ -208,6 +208,10 @@ void wide_destroy(WidePlan* p) {
 int wide_create(const DevModel& M, int C, WidePlan** out, double** coef64, double** part_lp, double** part_g,
                 std::string& err) {
   *out = nullptr;
+  if (C < 1 || C > 65535) {  // the epilogue's grid has one y-block per chain
+    err = "the wide-design gradient takes 1 to 65535 chains";
+    return GNUTS_ERR_ARGUMENT;
+  }
   WidePlan* p = new WidePlan();
   p->C = C;
   p->K = M.K;

@@ -365,6 +365,28 @@ def bench_learned(model_id, chains=256):
                         "divergence_rate": float(fl.draws[:, :, 5].mean()), "report": rep}}
 
 
+def run_profile_case(case):
+    """Short runs whose kernels the ncu summaries in profiles/ describe:
+    flow_hier_256 - the learned sampler's fused kernel (flow trained 50 steps
+    on the centered hierarchical model, then 256 chains x 20 + 10);
+    horseshoe_short - the wide-design gradient round (horseshoe, 256 chains,
+    5 + 2, mixed precision)."""
+    import cmdstan_gb300 as gn
+    from cmdstan_gb300 import workloads
+    if case == "flow_hier_256":
+        m = gn.Model("hier", workloads.hier(seed=0))
+        f = gn.Flow(m.dim)
+        f.init_affine(np.zeros(m.dim), np.ones(m.dim), seed=1)
+        f.train(m, steps=50, seed=3)
+        fit = m.sample_flow(f, num_chains=256, num_warmup=20, num_samples=10, seed=5)
+    else:
+        m = gn.Model("horseshoe", workloads.horseshoe(seed=0))
+        fit = m.sample(num_chains=256, num_warmup=5, num_samples=2, seed=3, precision=gn.PRECISION_MIXED, refresh=0)
+    print(json.dumps({"profile_case": case, "note": "profiling run, not a bench value",
+                      "timing": {k: float(v) for k, v in fit.timing.items()},
+                      "leapfrogs": int(fit.n_leapfrog.sum())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -377,9 +399,13 @@ def main():
                     help="skip the batched-posterior and funnel (learned vs plain) workloads")
     ap.add_argument("--quick", action="store_true",
                     help="profiling aid: one short run (20 warmup + 10 draws) of the same workload; not a bench value")
+    ap.add_argument("--profile-case", choices=["flow_hier_256", "horseshoe_short"],
+                    help="profiling aid: a short run of another workload's hot kernel; not a bench value")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return run_profile_case(args.profile_case)
     if args.quick:
         import cmdstan_gb300 as gn
         model = gn.Model("logistic", workload_data(0))

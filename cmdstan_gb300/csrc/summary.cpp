@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdint>
 #include <numeric>
+#include <utility>
 #include <thread>
 #include <vector>
 #include "../../include/gnuts.h"
@@ -170,44 +171,68 @@ Seqs split_of(const Seqs& in) {
   return out;
 }
 
-// normal scores of pooled ranks (average ranks for ties)
-Seqs zscale(const Seqs& in) {
+// normal scores of pooled ranks (average ranks for ties).  The draws are
+// sorted as contiguous (value, position) pairs: the order among equal values
+// does not matter, since tied draws share the mean of their ranks.
+// When sorted_out is given it receives the sorted values.
+Seqs zscale(const Seqs& in, std::vector<double>* sorted_out = nullptr) {
   const size_t S = in.data.size();
-  std::vector<uint32_t> idx(S);
-  std::iota(idx.begin(), idx.end(), 0u);
-  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return in.data[a] < in.data[b]; });
+  std::vector<std::pair<double, uint32_t>> vi(S);
+  for (size_t k = 0; k < S; ++k) vi[k] = {in.data[k], (uint32_t)k};
+  std::sort(vi.begin(), vi.end(),
+            [](const std::pair<double, uint32_t>& a, const std::pair<double, uint32_t>& b) { return a.first < b.first; });
+  if (sorted_out) {
+    sorted_out->resize(S);
+    for (size_t k = 0; k < S; ++k) (*sorted_out)[k] = vi[k].first;
+  }
   Seqs out = in;
   size_t i = 0;
   while (i < S) {
     size_t j = i + 1;
-    while (j < S && in.data[idx[j]] == in.data[idx[i]]) ++j;
+    while (j < S && vi[j].first == vi[i].first) ++j;
     const double rank = 0.5 * (double)(i + 1 + j);  // mean of ranks i+1 .. j
     const double z = ppnd16((rank - 0.375) / ((double)S + 0.25));
-    for (size_t k = i; k < j; ++k) out.data[idx[k]] = z;
+    for (size_t k = i; k < j; ++k) out.data[vi[k].second] = z;
     i = j;
   }
   return out;
+}
+
+// type-7 median of v (reordered in place) from its two order statistics
+double median_select(std::vector<double>& v) {
+  const double h = (v.size() - 1) * 0.5;
+  const size_t lo = (size_t)std::floor(h);
+  const size_t hi = std::min(lo + 1, v.size() - 1);
+  std::nth_element(v.begin(), v.begin() + lo, v.end());
+  const double a = v[lo];
+  const double b = hi == lo ? a : *std::min_element(v.begin() + lo + 1, v.end());
+  return a + (h - lo) * (b - a);
 }
 
 void summarize(const double* x, int M, int n, int64_t sc, int64_t si, const double* probs, int np, double* out) {
   Seqs S{M, n, std::vector<double>((size_t)M * n)};
   for (int m = 0; m < M; ++m)
     for (int i = 0; i < n; ++i) S.data[(size_t)m * n + i] = x[m * sc + i * si];
-  std::vector<double> sorted = S.data;
-  std::sort(sorted.begin(), sorted.end());
+  // split chains: with an even chain length they hold every draw, so the
+  // sort behind their normal scores also gives the pooled sorted values
+  const Seqs sp = split_of(S);
+  std::vector<double> sorted;
+  const Seqs zsp = zscale(sp, n % 2 == 0 ? &sorted : nullptr);
+  if (n % 2 != 0) {
+    sorted = S.data;
+    std::sort(sorted.begin(), sorted.end());
+  }
   const double mu = mean_of(S.data.data(), (int)S.data.size());
   const double sd = std::sqrt(var_of(S.data.data(), (int)S.data.size(), mu));
   const double med = quantile_sorted(sorted, 0.5);
   std::vector<double> dev(S.data.size());
   for (size_t i = 0; i < dev.size(); ++i) dev[i] = std::fabs(S.data[i] - med);
-  std::sort(dev.begin(), dev.end());
   out[0] = mu;
   out[1] = sd / std::sqrt(ess_of(S));
   out[2] = sd;
-  out[3] = 1.4826 * quantile_sorted(dev, 0.5);
+  out[3] = 1.4826 * median_select(dev);
   for (int k = 0; k < np; ++k) out[4 + k] = quantile_sorted(sorted, probs[k]);
-  const Seqs sp = split_of(S);
-  out[4 + np] = ess_of(zscale(sp));
+  out[4 + np] = ess_of(zsp);
   // tail ESS: indicators of the 5% and 95% quantiles
   const double q05 = quantile_sorted(sorted, 0.05), q95 = quantile_sorted(sorted, 0.95);
   Seqs i05 = sp, i95 = sp;
@@ -217,7 +242,7 @@ void summarize(const double* x, int M, int n, int64_t sc, int64_t si, const doub
   // R-hat: bulk on ranks, tail on ranks of |x - median|
   Seqs fold = sp;
   for (double& v : fold.data) v = std::fabs(v - med);
-  out[6 + np] = std::max(rhat_of(zscale(sp)), rhat_of(zscale(fold)));
+  out[6 + np] = std::max(rhat_of(zsp), rhat_of(zscale(fold)));
 }
 
 }  // namespace

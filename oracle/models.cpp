@@ -43,6 +43,23 @@ inline double inv_logit(double a) {
 
 enum Kind { BERN, NORMAL, LOGISTIC, HIER, FUNNEL, VARINT, HORSESHOE };
 
+// x . b in FP64 with four interleaved partial sums, ((s0 + s1) + (s2 + s3))
+// plus the tail: the row products of a GLM as a vectorising CPU library
+// forms them (a single running sum is one serial add chain per row)
+static double dot4(const double* x, const double* b, int D) {
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  int d = 0;
+  for (; d + 4 <= D; d += 4) {
+    s0 += x[d] * b[d];
+    s1 += x[d + 1] * b[d + 1];
+    s2 += x[d + 2] * b[d + 2];
+    s3 += x[d + 3] * b[d + 3];
+  }
+  double t = (s0 + s1) + (s2 + s3);
+  for (; d < D; ++d) t += x[d] * b[d];
+  return t;
+}
+
 }  // namespace
 
 struct orc_model {
@@ -136,8 +153,7 @@ double orc_log_prob_grad(const orc_model* m, const double* q, int jac, double* g
       for (int d = 0; d <= D; ++d) g[d] = 0;
       for (int n = 0; n < N; ++n) {
         const double* x = &m->X[(size_t)n * D];
-        double eta = alpha;
-        for (int d = 0; d < D; ++d) eta += x[d] * beta[d];
+        const double eta = alpha + dot4(x, beta, D);
         int y = m->yi[n];
         lp += y * eta - log1p_exp(eta);
         double r = y - inv_logit(eta);
@@ -260,8 +276,7 @@ double orc_log_prob_grad(const orc_model* m, const double* q, int jac, double* g
       double lp = 0, gb0 = 0;
       for (int n = 0; n < N; ++n) {
         const double* x = &m->X[(size_t)n * D];
-        double eta = b0;
-        for (int d = 0; d < D; ++d) eta += x[d] * beta[d];
+        const double eta = b0 + dot4(x, beta.data(), D);
         int y = m->yi[n];
         lp += y * eta - log1p_exp(eta);
         double r = y - inv_logit(eta);

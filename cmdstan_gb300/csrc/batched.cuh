@@ -32,13 +32,15 @@ struct GradOut {
   float* coef32;    // [C][K+1]
   double* part_lp;  // [S][C]
   double* part_g;   // [S][C][K+1] (SIMT path)
-  float* part_g32;  // [S][C][TC_GSTRIDE] (tensor-core path: FP32 accumulators)
+  float* part_g32;  // [S][C][TC_GSTRIDE] (tensor-core path: FP32 accumulators; position k < K is
+                    // beta_k, position K the intercept, as the tensor-core columns are ordered)
   const int* done_count;
   int C_total;
   void* tc;           // tensor-core plan (grad_tc.cu), null for the SIMT path
   void* wide;         // cuBLASLt plan for wide designs (grad_wide.cu), or null
   uint16_t* coef_bf;  // tensor-core operand: [2][Cpad][128] BF16 hi / lo planes
   int Cpad;
+  double* lin;        // [C] tensor-core path: linear likelihood part (hi + lo) . xtc_ym
 };
 
 // Sum the S row-split partials of chain c in a fixed order (s = 0, 1, ...):
@@ -78,9 +80,10 @@ __device__ __forceinline__ void sum_splits(const GradOut& G, int c, double* out,
     }
   }
 }
-// Tensor-core partials: lane l owns coefficients 4l .. 4l+3 and loads one
+// Tensor-core partials: lane l owns positions 4l .. 4l+3 and loads one
 // 16-byte vector per split, all splits in flight at once, summed in split
 // order in FP32 (the same values and order as the FP64-stored path).
+// Position p < K is beta_p (out[1 + p]), position K the intercept (out[0]).
 __device__ __forceinline__ void sum_splits_f32(const GradOut& G, int c, double* out, int lane) {
   const float4* src = reinterpret_cast<const float4*>(G.part_g32 + (size_t)c * TC_GSTRIDE) + lane;
   const size_t stride = (size_t)G.C * TC_GSTRIDE / 4;
@@ -100,11 +103,13 @@ __device__ __forceinline__ void sum_splits_f32(const GradOut& G, int c, double* 
         a.w += v[u].w;
       }
   }
-  const int i = 4 * lane;
-  if (i <= G.K) out[i] = (double)a.x;
-  if (i + 1 <= G.K) out[i + 1] = (double)a.y;
-  if (i + 2 <= G.K) out[i + 2] = (double)a.z;
-  if (i + 3 <= G.K) out[i + 3] = (double)a.w;
+  const float av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int p = 4 * lane + j;
+    if (p < G.K) out[1 + p] = (double)av[j];
+    else if (p == G.K) out[0] = (double)av[j];
+  }
 }
 
 // lp partials of chain c summed in FP64, same order on every lane
@@ -135,15 +140,23 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
   if (M.kind == MK_LOGISTIC) {
     if (G.coef_bf) {
       // tensor-core operand: column k < K -> beta_k, column K -> intercept (it
-      // meets the ones column of X), split v = hi + lo in BF16
+      // meets the ones column of X), split v = hi + lo in BF16.  The kernel
+      // sums only the even part of the likelihood; its linear part
+      // sum_n (y_n - 1/2) eta_n = (hi + lo) . Xtc^T (y - 1/2) is formed here,
+      // in FP64, for exactly the coefficients the kernel multiplies.
       __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(G.coef_bf) + (size_t)c * 128;
       __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(G.coef_bf) + ((size_t)G.Cpad + c) * 128;
+      double lin = 0;
       for (int i = lane; i < 128; i += 32) {
         double v = i < K ? q[1 + i] : (i == K ? q[0] : 0.0);
         __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+        __nv_bfloat16 l = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
         hi[i] = h;
-        lo[i] = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
+        lo[i] = l;
+        if (i < XTC_LD) lin += ((double)__bfloat162float(h) + (double)__bfloat162float(l)) * M.xtc_ym[i];
       }
+      lin = wsum(lin);
+      if (lane == 0) G.lin[c] = lin;
       return;
     }
     for (int i = lane; i <= K; i += 32) {
@@ -178,6 +191,7 @@ __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevMod
   else if (G.prec == GNUTS_PRECISION_FP64) sum_splits<double>(G, c, g, lane);
   else sum_splits<float>(G, c, g, lane);
   double lp = sum_split_lp(G, c);
+  if (G.lin) lp += G.lin[c];
   __syncwarp();
   const double* gs = g;
   if (M.kind == MK_LOGISTIC) {

@@ -3,12 +3,24 @@
 // Per round every live chain c needs, for its coefficients B_c (intercept
 // folded in through a ones column of X),
 //     H[c, n] = B_c . X_n                       GEMM1, M = chains, N = rows, K = predictors
-//     lp_c    = -sum_n softplus(s_n H[c, n]),   s_n = 1 - 2 y_n
-//     R[c, n] = -s_n inv_logit(s_n H[c, n])     (= y_n - inv_logit(H[c, n]))
+//     lp_c    = sum_n y_n H[c, n] - softplus(H[c, n])
+//     R[c, n] = y_n - inv_logit(H[c, n])
 //     G[c, k] = sum_n R[c, n] X[n, k]           GEMM2, M = chains, N = predictors, K = rows
 // which is the reverse sweep Stan Math performs for one chain's
 // bernoulli_logit likelihood (log_prob_grad contract, src/cmdstan/
 // command_helper.hpp:589-593), done for 128 chains at once.
+//
+// The likelihood is split into a linear and an even part,
+//     y h - softplus(h) = (y - 1/2) h  -  (|h|/2 + log1p(exp(-|h|))),
+// and the linear part summed over rows is B_c . v with v = X^T (y - 1/2), a
+// vector fixed by the data: stage_request forms that dot product in FP64 for
+// the exact BF16 hi + lo coefficients this kernel multiplies, so the kernel
+// only sums the even part.  Per element it then takes one ex2 (e =
+// exp(-|h|)); the log1p terms of a thread's 32-row slice are summed as one
+// lg2 of the product of their (1 + e) factors (at most 2^32), and the
+// inverse-logit shares one reciprocal between four rows (1/d_i from
+// 1/(d_0 d_1 d_2 d_3) and the partial products): 1.28 special-function
+// operations per element (ex2, a quarter rcp, 1/32 lg2) instead of three.
 //
 // Precision: X is BF16-exact (the workload's design matrix is defined on
 // BF16 values).  Coefficients are split hi + lo in BF16, so GEMM1 is two BF16
@@ -17,21 +29,35 @@
 // BF16 (relative error 2^-9 per residual, about 1e-3 on a gradient
 // component); a gradient error leaves the leapfrog volume preserving and
 // reversible and lp is computed separately, so it does not bias the target.
-// softplus / inv_logit run in FP32; each thread sums its 32-row slice of lp
-// in FP32 (four interleaved partial sums) and the slices of successive tiles
+// The even part runs in FP32; each thread's slice sum is added to its total
 // with Kahan-compensated FP32 additions; the reduction over the 512 threads'
-// totals and over row splits is FP64.
+// totals and over row splits is FP64, and so is the linear part.
+//
+// X rows carry 104 BF16 columns (K predictors, the ones column, zeros), so
+// GEMM1 runs 7 K-steps of 16 (112 columns) and GEMM2 has N = 112.
 //
 // CTA = one 128-chain tile x one row split, 576 threads:
-//   warp 0       TMA producer: coefficient hi/lo tiles once, X row tiles
-//                (2-stage ring, 128 rows x 128 predictors, SWIZZLE_128B)
+//   warp 0       TMA producer: X row tiles (6-stage ring, 128 rows x 128
+//                predictors, SWIZZLE_128B)
 //   warp 1       MMA issuer (one thread) + TMEM owner
 //   warps 2..17  epilogue: thread = (chain, 32-row slice of the tile), four
-//                warps per TMEM lane quadrant; reads its H slice from TMEM,
-//                writes R into one of two shared-memory buffers in the SW128
-//                K-major layout GEMM2 reads; y of the split is staged as floats
-// TMEM: H double buffer (2 x 128 columns) + G (128 columns).  With H and R
-// double-buffered, GEMM1 of tile t+1 and GEMM2 of tile t-1 run while the
+//                warps per TMEM lane quadrant; reads its H slice from TMEM and
+//                writes its 32 BF16 residuals back over the first 16 columns
+//                of that slice; y - 1/2 of the split is staged as floats
+// TMEM (512 columns): two H buffers (128 each; each also carries the
+// residuals of its tile, GEMM2's A operand: lane = chain, two BF16 rows per
+// column), G (112, at 256), and the coefficient tile as GEMM1's A operand
+// (hi and lo planes, 56 columns each), written once per launch by the
+// epilogue warps with tcgen05.st.  Both A operands live in TMEM, so shared
+// memory holds only the X ring: an X tile is held from its load until GEMM2
+// of that tile retires (across GEMM1, the epilogue and GEMM2), and six stages
+// keep the next loads in flight behind the L2 latency (with two, the loads
+// sat on the critical path).  The MMA thread issues GEMM2 of tile t before
+// GEMM1 of tile t + 2, which overwrites the same buffer; tcgen05.mma
+// operations of one thread execute in issue order, so no barrier is needed
+// between the residual reads and that overwrite, nor between the epilogue's
+// reads of H and its residual writes (the slice's own columns, after
+// tcgen05.wait::ld).  GEMM1 of tile t+1 and GEMM2 of tile t-1 run while the
 // epilogue works on tile t.
 // Every mbarrier wait is bounded; on expiry the kernel records an error,
 // drains what it issued and frees TMEM.
@@ -47,27 +73,33 @@ namespace {
 
 constexpr int TILE_BYTES = 128 * 128 * 2;   // [2 k-halves][128 rows][64] BF16
 constexpr int HALF_BYTES = TILE_BYTES / 2;  // one k-half: 128 rows x 128 B
-constexpr int NS = 2;
+constexpr int NS = 6;
 constexpr int EPI_WARPS = 16;                 // 4 per TMEM lane quadrant, 32 rows each
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr int MAX_SPLIT_ROWS = 6144;          // y of a whole row split staged as floats
-constexpr int OFF_CHI = 0;
-constexpr int OFF_CLO = OFF_CHI + TILE_BYTES;
-constexpr int OFF_X = OFF_CLO + TILE_BYTES;
-constexpr int OFF_R = OFF_X + NS * TILE_BYTES;  // 2 residual buffers (BF16)
-constexpr int OFF_BAR = OFF_R + 2 * TILE_BYTES;  // 16 barriers
-constexpr int OFF_MISC = OFF_BAR + 16 * 8;     // tmem base, abort flag
+constexpr int OFF_X = 0;
+constexpr int OFF_BAR = OFF_X + NS * TILE_BYTES;  // 24 barriers
+constexpr int OFF_MISC = OFF_BAR + 24 * 8;     // tmem base, abort flag
 constexpr int OFF_LP = OFF_MISC + 16;          // [4][128] doubles
 constexpr int OFF_Y = OFF_LP + 4 * 128 * 8;    // [MAX_SPLIT_ROWS] floats
 constexpr int SMEM_USED = OFF_Y + MAX_SPLIT_ROWS * 4;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;   // alignment slack
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
+// K-steps of 16 columns that cover an X row of XTC_LD columns, and GEMM2's N
+constexpr int KSTEPS = (XTC_LD + 15) / 16;
+constexpr uint32_t GN = 16u * KSTEPS;
+static_assert(KSTEPS <= 8 && GN % 16 == 0, "X rows fit the 128-column tile");
+// TMEM columns: H buffers at 0 and 128, G at 256, coefficient planes after
+constexpr uint32_t TM_G = 256;
+constexpr uint32_t ACOLS = 8 * KSTEPS;        // one plane of A: GN BF16 per lane
+constexpr uint32_t TM_AHI = 384, TM_ALO = TM_AHI + ACOLS;
+static_assert(TM_ALO + ACOLS <= TMEM_COLS && TM_G + 128 <= TM_AHI, "TMEM column map");
+static_assert(ACOLS / 2 == 28, "each half-plane is written as x16 + x8 + x4 columns");
 
 // barrier indices
-enum { B_XFULL = 0, B_XEMPTY = NS, B_CFULL = 2 * NS, B_HFULL, B_HFULL1, B_HEMPTY, B_HEMPTY1, B_RFULL, B_RFULL1,
-       B_REMPTY, B_REMPTY1, B_GDONE, B_DRAIN };
-static_assert(B_DRAIN < 16, "barrier area holds 16 barriers");
+enum { B_XFULL = 0, B_XEMPTY = NS, B_HFULL = 2 * NS, B_HFULL1, B_RFULL, B_RFULL1, B_GDONE, B_DRAIN, B_AREADY };
+static_assert(B_AREADY < 24, "barrier area holds 24 barriers");
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -119,17 +151,22 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t 
   d |= (uint64_t)2 << 61;
   return d;
 }
-// instruction descriptor, kind::f16: D FP32, A/B BF16, M = 128, N = 128
-__host__ __device__ constexpr uint32_t idesc(bool a_mn, bool b_mn) {
+// instruction descriptor, kind::f16: D FP32, A/B BF16, M = 128, N = n (a multiple of 16)
+__host__ __device__ constexpr uint32_t idesc(bool a_mn, bool b_mn, uint32_t n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
-         ((128u >> 3) << 17) | ((128u >> 4) << 24);
+         ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t accum) {
+// A from tensor memory (lane = row of A, two BF16 per 32-bit column); the B
+// descriptor is passed as its two 32-bit halves: the issuing thread forms the
+// low half with one add per MMA (the address field is its low 14 bits and a
+// stage's addresses never carry out of it), the high half is fixed.
+__device__ __forceinline__ void mma_ta(uint32_t d, uint32_t a_tmem, uint32_t b_lo, uint32_t b_hi, uint32_t id,
+                                       uint32_t accum) {
   asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-      "l"(a), "l"(b), "r"(id), "r"(accum)
+      "{\n\t.reg .pred p;\n\t.reg .b64 bd;\n\tsetp.ne.b32 p, %5, 0;\n\tmov.b64 bd, {%2, %3};\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], bd, %4, p;\n\t}" ::"r"(d),
+      "r"(a_tmem), "r"(b_lo), "r"(b_hi), "r"(id), "r"(accum)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
@@ -147,6 +184,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* r) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t* r) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(r[0]), "r"(r[1]),
+               "r"(r[2]), "r"(r[3])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // single-instruction approximations (SFU): 2^x, log2(x), 1/x
 __device__ __forceinline__ float ex2a(float x) {
@@ -172,15 +228,16 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 
 struct TcArgs {
   int N, K, C, Cpad, rows_per_split, S, C_total;
+  const uint16_t* coef;  // [2][Cpad][128] BF16 hi / lo planes (stage_request)
   const uint32_t* ybits;
   double* part_lp;
-  float* part_g;  // [S][C][TC_GSTRIDE]: coefficient 0 = intercept, 1 + k = beta_k
+  float* part_g;  // [S][C][TC_GSTRIDE]: position k < K = beta_k, K = intercept, zeros after
   const int* done_count;
   int* error;
 };
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
-    k_glm_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap cmap, TcArgs A) {
+    k_glm_tc(const __grid_constant__ CUtensorMap xmap, TcArgs A) {
   if (A.done_count && *A.done_count >= A.C_total) return;
   extern __shared__ uint8_t smem_raw[];
   // SWIZZLE_128B tiles need 1024-byte alignment in the shared address space
@@ -202,17 +259,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       mbar_init(bar(B_XFULL + s), 1);
       mbar_init(bar(B_XEMPTY + s), 1);
     }
-    mbar_init(bar(B_CFULL), 1);
     mbar_init(bar(B_HFULL), 1);
     mbar_init(bar(B_HFULL1), 1);
-    mbar_init(bar(B_HEMPTY), EPI_WARPS);
-    mbar_init(bar(B_HEMPTY1), EPI_WARPS);
     mbar_init(bar(B_RFULL), EPI_WARPS);
     mbar_init(bar(B_RFULL1), EPI_WARPS);
-    mbar_init(bar(B_REMPTY), 1);
-    mbar_init(bar(B_REMPTY1), 1);
     mbar_init(bar(B_GDONE), 1);
     mbar_init(bar(B_DRAIN), 1);
+    mbar_init(bar(B_AREADY), EPI_WARPS);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -226,16 +279,36 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = *tmem_slot;
+  if (warp >= 2) {
+    // GEMM1's A operand into TMEM: warp (quadrant q, sub) writes lanes 32q..32q+31
+    // (chains c0 + 32q + lane), plane sub >> 1 (hi, lo), columns of half sub & 1
+    const int q = warp & 3, sub = (warp - 2) >> 2;
+    const int plane = sub >> 1, half = sub & 1;
+    const uint4* src = reinterpret_cast<const uint4*>(
+        A.coef + ((size_t)(plane ? A.Cpad : 0) + c0 + q * 32 + lane) * 128 + half * (ACOLS / 2) * 2);
+    uint32_t r[ACOLS / 2];
+#pragma unroll
+    for (int i = 0; i < (int)ACOLS / 8; ++i) {
+      const uint4 u = src[i];
+      r[4 * i] = u.x;
+      r[4 * i + 1] = u.y;
+      r[4 * i + 2] = u.z;
+      r[4 * i + 3] = u.w;
+    }
+    const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (plane ? TM_ALO : TM_AHI) + half * (ACOLS / 2);
+    tmem_st16(ta, r);
+    tmem_st8(ta + 16, r + 16);
+    tmem_st4(ta + 24, r + 24);
+    tmem_wait_st();
+    fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(bar(B_AREADY));  // the MMA thread waits for all 16 before GEMM1
+  }
 
   if (warp == 0) {
     // ---------------- TMA producer
     if (lane == 0) {
       int issued = 0;
-      mbar_expect_tx(bar(B_CFULL), 2 * TILE_BYTES);
-      tma_load_2d(sbase + OFF_CHI, &cmap, 0, c0, bar(B_CFULL));
-      tma_load_2d(sbase + OFF_CHI + HALF_BYTES, &cmap, 64, c0, bar(B_CFULL));
-      tma_load_2d(sbase + OFF_CLO, &cmap, 0, A.Cpad + c0, bar(B_CFULL));
-      tma_load_2d(sbase + OFF_CLO + HALF_BYTES, &cmap, 64, A.Cpad + c0, bar(B_CFULL));
       for (int t = 0; t < T; ++t) {
         const int s = t % NS;
         if (t >= NS && !mbar_wait(bar(B_XEMPTY + s), ((t / NS) - 1) & 1, abort)) break;
@@ -251,49 +324,48 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           volatile int never = 0;
           mbar_wait(bar(B_XFULL + t % NS), (t / NS) & 1, &never);
         }
-        volatile int never = 0;
-        mbar_wait(bar(B_CFULL), 0, &never);
       }
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      const uint32_t ID1 = idesc(false, false);  // A coef K-major, B = X K-major
-      const uint32_t ID2 = idesc(false, true);   // A = R K-major, B = X MN-major
-      const uint32_t tG = tmem + 256;
-      bool ok = mbar_wait(bar(B_CFULL), 0, abort);
-      // GEMM2 of tile u: G += R(u) . X(u), R in residual buffer u & 1
+      const uint32_t ID1 = idesc(false, false, 128);  // A coef (TMEM), B = X K-major (N = 128 rows)
+      const uint32_t ID2 = idesc(false, true, GN);    // A = R (TMEM), B = X MN-major (N = GN predictors)
+      const uint32_t tG = tmem + TM_G;
+      bool ok = mbar_wait(bar(B_AREADY), 0, abort);
+      // B descriptors of X stage 0: K-major for GEMM1, MN-major for GEMM2
+      const uint64_t d1 = sdesc(sbase + OFF_X, 0, 1024), d2 = sdesc(sbase + OFF_X, HALF_BYTES, 1024);
+      const uint32_t d1lo = (uint32_t)d1, d1hi = (uint32_t)(d1 >> 32);
+      const uint32_t d2lo = (uint32_t)d2, d2hi = (uint32_t)(d2 >> 32);
+      // GEMM2 of tile u: G += R(u) . X(u); rows 16i .. 16i + 15 of R sit in
+      // columns 8i .. 8i + 7 of slice i / 2 (slice j starts at column 32 j)
       auto gemm2 = [&](int u) -> bool {
         const int rb = u & 1;
         if (!mbar_wait(bar(B_RFULL + rb), (u >> 1) & 1, abort)) return false;
         fence_after();
-        const uint32_t xs = sbase + OFF_X + (u % NS) * TILE_BYTES;
-        const uint32_t rs = sbase + OFF_R + rb * TILE_BYTES;
+        const uint32_t xlo = d2lo + (uint32_t)(((u % NS) * TILE_BYTES) >> 4);
+        const uint32_t tR = tmem + rb * 128;
+        const uint32_t acc0 = u > 0 ? 1u : 0u;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          uint64_t a = sdesc(rs + (i >> 2) * HALF_BYTES + (i & 3) * 32, 0, 1024);
-          uint64_t b = sdesc(xs + i * 2048, HALF_BYTES, 1024);
-          mma(tG, a, b, ID2, (u > 0 || i > 0) ? 1u : 0u);
-        }
+        for (int i = 0; i < 8; ++i)
+          mma_ta(tG, tR + (i >> 1) * 32 + (i & 1) * 8, xlo + (uint32_t)((i * 2048) >> 4), d2hi, ID2, i > 0 ? 1u : acc0);
         mma_commit(bar(B_XEMPTY + u % NS));
-        mma_commit(bar(B_REMPTY + rb));
         return true;
       };
       int t = 0;
       for (; ok && t < T; ++t) {
         const int s = t % NS, b = t & 1;
         if (!mbar_wait(bar(B_XFULL + s), (t / NS) & 1, abort)) { ok = false; break; }
-        if (t >= 2 && !mbar_wait(bar(B_HEMPTY + b), ((t >> 1) - 1) & 1, abort)) { ok = false; break; }
         fence_after();
-        const uint32_t xs = sbase + OFF_X + s * TILE_BYTES;
+        const uint32_t xlo = d1lo + (uint32_t)((s * TILE_BYTES) >> 4);
         const uint32_t tH = tmem + b * 128;
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
-          const uint32_t cs = sbase + (part ? OFF_CLO : OFF_CHI);
+          const uint32_t ta = tmem + (part ? TM_ALO : TM_AHI);
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
+          for (int i = 0; i < KSTEPS; ++i) {
             const uint32_t koff = (i >> 2) * HALF_BYTES + (i & 3) * 32;
-            mma(tH, sdesc(cs + koff, 0, 1024), sdesc(xs + koff, 0, 1024), ID1, (part > 0 || i > 0) ? 1u : 0u);
+            mma_ta(tH, ta + 8 * i, xlo + (koff >> 4), d1hi, ID1, (part > 0 || i > 0) ? 1u : 0u);
           }
         }
         mma_commit(bar(B_HFULL + b));
@@ -314,18 +386,36 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int c = c0 + cl;
     const int et = threadIdx.x - 64;    // 0 .. 511
     float* ys = (float*)(smem + OFF_Y);
-    // stage y of this row split as 0/1 floats (read back as warp-wide broadcasts)
-    for (int i = et; i < T * 128; i += 32 * EPI_WARPS) {
-      const int n = row_begin + i;
-      ys[i] = (n < row_end && ((A.ybits[n >> 5] >> (n & 31)) & 1u)) ? 1.f : 0.f;
+    // stage y - 1/2 of this row split as floats (read back as warp-wide
+    // broadcasts).  Thread et writes float4 number f = et + 512 k (rows 4f ..
+    // 4f + 3, from packed word f / 8: row_begin is a multiple of 128); the
+    // loads of a thread's four float4 are issued together.  Rows past the data
+    // have zero bits (the packed words are zero-padded), i.e. y - 1/2 = -1/2.
+    {
+      const uint32_t* yw = A.ybits + (row_begin >> 5);
+      const int nf = T * 32;  // float4 count: 128 rows per tile
+      for (int f0 = et; f0 < nf; f0 += 4 * 32 * EPI_WARPS) {
+        uint32_t w[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int f = f0 + k * 32 * EPI_WARPS;
+          w[k] = f < nf ? yw[f >> 3] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int f = f0 + k * 32 * EPI_WARPS;
+          const uint32_t bb = w[k] >> (4 * (f & 7));
+          if (f < nf)
+            reinterpret_cast<float4*>(ys)[f] = make_float4((bb & 1u) ? 0.5f : -0.5f, (bb & 2u) ? 0.5f : -0.5f,
+                                                           (bb & 4u) ? 0.5f : -0.5f, (bb & 8u) ? 0.5f : -0.5f);
+        }
+      }
     }
     asm volatile("bar.sync 1, 512;" ::: "memory");
     // the slice sums of successive tiles are added in FP32 with Kahan
     // compensation (no FP64 instruction per tile on this part's narrow FP64
     // pipe); the thread's total becomes FP64 once, at the end
     float lp_acc = 0.f, lp_comp = 0.f;
-    const int kh = sub >> 1;            // k-half of the R tile this slice lands in
-    uint8_t* rrow = smem + OFF_R + kh * HALF_BYTES + cl * 128;
     bool ok = true;
     for (int t = 0; t < T && ok; ++t) {
       const int b = t & 1;
@@ -336,95 +426,84 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       tmem_ld16(ta, v);
       tmem_ld16(ta + 16, v + 16);
       tmem_wait_ld();
-      fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(bar(B_HEMPTY + b));
       const int r0 = row_begin + t * 128 + sub * 32;
       const float4* y4 = reinterpret_cast<const float4*>(ys + t * 128 + sub * 32);
       const int nvalid = row_end - r0;  // >= 32 on every tile but the last
-      float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+      if (nvalid < 32) {
+        // rows past the data: their X rows are TMA zero fill, so h = 0 there;
+        // with h set to +0 each contributes a factor 1 + 2^0 = 2 to the
+        // product and nothing to the |h| sum (R there meets a zero X row)
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = j < nvalid ? v[j] : 0.f;
+      }
+      // products of (1 + e) over alternate quads (each at most 2^16), |h| sums
+      float pr0 = 1.f, pr1 = 1.f, sa0 = 0.f, sa1 = 0.f;
       uint32_t hi[16];
-#define GN_EPI_ELEMENT(J, Y, R, ACC)                                               \
-      {                                                                            \
-        const float eta = v[J];                                                    \
-        const float ex = ex2a(-1.4426950408889634f * fabsf(eta));                  \
-        const float d = 1.f + ex;                                                  \
-        const float sp = fmaf(lg2a(d), 0.69314718055994531f, fmaxf(eta, 0.f));     \
-        const float inv = rcpa(d);                                                 \
-        const float sig = (eta >= 0.f ? 1.f : ex) * inv;                           \
-        ACC += fmaf(Y, eta, -sp);                                                  \
-        R = Y - sig;                                                               \
-      }
-      if (nvalid >= 32) {
 #pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 yv = y4[j4];
-          float r0v, r1v, r2v, r3v;
-          GN_EPI_ELEMENT(4 * j4 + 0, yv.x, r0v, acc0)
-          GN_EPI_ELEMENT(4 * j4 + 1, yv.y, r1v, acc1)
-          GN_EPI_ELEMENT(4 * j4 + 2, yv.z, r2v, acc2)
-          GN_EPI_ELEMENT(4 * j4 + 3, yv.w, r3v, acc3)
-          hi[2 * j4] = pack_bf16(r0v, r1v);
-          hi[2 * j4 + 1] = pack_bf16(r2v, r3v);
+      for (int j4 = 0; j4 < 8; ++j4) {
+        const float4 yv = y4[j4];  // y - 1/2
+        const float x0 = v[4 * j4], x1 = v[4 * j4 + 1], x2 = v[4 * j4 + 2], x3 = v[4 * j4 + 3];
+        const float d0 = 1.f + ex2a(-1.4426950408889634f * fabsf(x0));
+        const float d1 = 1.f + ex2a(-1.4426950408889634f * fabsf(x1));
+        const float d2 = 1.f + ex2a(-1.4426950408889634f * fabsf(x2));
+        const float d3 = 1.f + ex2a(-1.4426950408889634f * fabsf(x3));
+        const float p01 = d0 * d1, p23 = d2 * d3;
+        const float pq = p01 * p23;
+        const float rq = rcpa(pq);
+        const float r01 = p23 * rq, r23 = p01 * rq;  // 1 / (d0 d1), 1 / (d2 d3)
+        // inv_logit(|h|) - 1/2 = 1/d - 1/2, and
+        // y - inv_logit(h) = (y - 1/2) - sign(h) (inv_logit(|h|) - 1/2)
+        const float w0 = fmaf(d1, r01, -0.5f), w1 = fmaf(d0, r01, -0.5f);
+        const float w2 = fmaf(d3, r23, -0.5f), w3 = fmaf(d2, r23, -0.5f);
+        const float R0 = yv.x - copysignf(w0, x0), R1 = yv.y - copysignf(w1, x1);
+        const float R2 = yv.z - copysignf(w2, x2), R3 = yv.w - copysignf(w3, x3);
+        if (j4 & 1) {
+          pr1 *= pq;
+          sa1 += (fabsf(x0) + fabsf(x1)) + (fabsf(x2) + fabsf(x3));
+        } else {
+          pr0 *= pq;
+          sa0 += (fabsf(x0) + fabsf(x1)) + (fabsf(x2) + fabsf(x3));
         }
-      } else {
-#pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 yv = y4[j4];
-          float rv[4];
-          const float yy[4] = {yv.x, yv.y, yv.z, yv.w};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            float a = 0.f, r;
-            GN_EPI_ELEMENT(4 * j4 + e, yy[e], r, a)
-            const bool valid = 4 * j4 + e < nvalid;
-            rv[e] = valid ? r : 0.f;
-            acc0 += valid ? a : 0.f;
-          }
-          hi[2 * j4] = pack_bf16(rv[0], rv[1]);
-          hi[2 * j4 + 1] = pack_bf16(rv[2], rv[3]);
-        }
+        hi[2 * j4] = pack_bf16(R0, R1);
+        hi[2 * j4 + 1] = pack_bf16(R2, R3);
       }
-#undef GN_EPI_ELEMENT
       {
-        const float yk = ((acc0 + acc1) + (acc2 + acc3)) - lp_comp;
+        // this slice's even part: sum |h|/2 + ln(prod (1 + e)); each row past
+        // the data contributed exactly one factor 2 and nothing to |h|
+        float l2 = lg2a(pr0 * pr1);
+        if (nvalid < 32) l2 -= (float)(32 - max(nvalid, 0));
+        const float yk = -fmaf(l2, 0.69314718055994531f, 0.5f * (sa0 + sa1)) - lp_comp;
         const float tk = lp_acc + yk;
         lp_comp = (tk - lp_acc) - yk;
         lp_acc = tk;
       }
-      // residual buffer t & 1 is free once GEMM2 of tile t - 2 has completed
-      if (t >= 2 && !mbar_wait(bar(B_REMPTY + b), ((t >> 1) - 1) & 1, abort)) { ok = false; break; }
-      // row cl of the K-major SW128 residual tile: 4 chunks of 8 rows' values
-      uint8_t* rdst = rrow + b * TILE_BYTES;
-#pragma unroll
-      for (int c4 = 0; c4 < 4; ++c4) {
-        const int pc = ((((sub & 1) * 4 + c4) ^ (cl & 7)) * 16);
-        *reinterpret_cast<uint4*>(rdst + pc) = make_uint4(hi[4 * c4], hi[4 * c4 + 1], hi[4 * c4 + 2], hi[4 * c4 + 3]);
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      // the slice's residuals, two BF16 rows per column, over its first 16 columns
+      tmem_st16(ta, hi);
+      tmem_wait_st();
+      fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(bar(B_RFULL + b));
     }
-    // G readout: 32 predictor columns per thread
-    if (ok && T > 0 && mbar_wait(bar(B_GDONE), 0, abort)) {
-      fence_after();
+    // G readout: 32 columns per thread, stored in TMEM column order (position
+    // k < K: beta_k, position K: intercept, zeros after) as 16-byte vectors, so
+    // each thread writes 128 contiguous bytes of its chain's row
+    {
       float g[32];
-      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + 256 + sub * 32;
-      tmem_ld16(ta, g);
-      tmem_ld16(ta + 16, g + 16);
-      tmem_wait_ld();
-      if (c < A.C) {
-        float* pg = A.part_g + ((size_t)split * A.C + c) * TC_GSTRIDE;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int k = sub * 32 + j;
-          if (k < A.K) pg[1 + k] = g[j];
-          else if (k == A.K) pg[0] = g[j];
-        }
+      const bool have = ok && T > 0 && mbar_wait(bar(B_GDONE), 0, abort);
+      if (have) {
+        fence_after();
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + TM_G + sub * 32;
+        tmem_ld16(ta, g);
+        tmem_ld16(ta + 16, g + 16);
+        tmem_wait_ld();
       }
-    } else if (T == 0 && c < A.C) {
-      float* pg = A.part_g + ((size_t)split * A.C + c) * TC_GSTRIDE;
-      for (int k = sub; k <= A.K; k += 4) pg[k] = 0.f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) g[j] = (have && sub * 32 + j <= A.K) ? g[j] : 0.f;
+      if (c < A.C && (have || T == 0)) {
+        float4* pg = reinterpret_cast<float4*>(A.part_g + ((size_t)split * A.C + c) * TC_GSTRIDE + sub * 32);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) pg[j] = make_float4(g[4 * j], g[4 * j + 1], g[4 * j + 2], g[4 * j + 3]);
+      }
     }
     lpx[sub * 128 + cl] = (double)lp_acc - (double)lp_comp;
     asm volatile("bar.sync 1, 512;" ::: "memory");
@@ -480,19 +559,22 @@ int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer,
 }  // namespace
 
 struct TcPlan {
-  CUtensorMap xmap, cmap;
+  CUtensorMap xmap;
   TcArgs args;
   dim3 grid;
   uint16_t* coef = nullptr;
   int* error = nullptr;
   double* part_lp = nullptr;
   float* part_g = nullptr;
+  double* lin = nullptr;
 };
 
-bool tc_supported(const DevModel& M) { return M.kind == MK_LOGISTIC && M.Xtc && M.K + 1 <= XTC_LD; }
+bool tc_supported(const DevModel& M) {
+  return M.kind == MK_LOGISTIC && M.Xtc && M.xtc_ym && M.K + 1 <= XTC_LD;
+}
 
 int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uint16_t** coef_bf, int* S_out,
-              double** part_lp, float** part_g, std::string& err) {
+              double** part_lp, float** part_g, double** lin, std::string& err) {
   if (!tc_supported(M)) {
     err = "tensor-core gradient needs a logistic model with at most 103 predictors";
     return GNUTS_ERR_ARGUMENT;
@@ -518,18 +600,19 @@ int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uin
   if ((e = cudaMalloc(&p->error, sizeof(int))) != cudaSuccess) return fail(e);
   cudaMemset(p->error, 0, sizeof(int));
   if ((e = cudaMalloc(&p->part_lp, sizeof(double) * S * C)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&p->lin, sizeof(double) * C)) != cudaSuccess) return fail(e);
+  cudaMemset(p->lin, 0, sizeof(double) * C);
   // padded to TC_GSTRIDE floats per chain (entries past K stay zero) so the
   // consumer sums whole 16-byte vectors
   if ((e = cudaMalloc(&p->part_g, sizeof(float) * S * C * TC_GSTRIDE)) != cudaSuccess) return fail(e);
   cudaMemset(p->part_g, 0, sizeof(float) * S * C * TC_GSTRIDE);
   int rc = make_map(&p->xmap, M.Xtc, XTC_LD, (uint64_t)M.N, XTC_LD * 2, err);
-  if (!rc) rc = make_map(&p->cmap, p->coef, 128, (uint64_t)2 * Cpad, 256, err);
   if (rc) {
     tc_destroy(p);
     return rc;
   }
-  p->args = TcArgs{M.N, M.K, C, Cpad, tiles_per_split * 128, S, C, M.ybits, p->part_lp, p->part_g, done_count,
-                   p->error};
+  p->args = TcArgs{M.N, M.K, C, Cpad, tiles_per_split * 128, S, C, p->coef, M.ybits, p->part_lp, p->part_g,
+                   done_count, p->error};
   p->grid = dim3(ctiles, S);
   if ((e = cudaFuncSetAttribute(k_glm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)) != cudaSuccess)
     return fail(e);
@@ -538,6 +621,7 @@ int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uin
   *S_out = S;
   *part_lp = p->part_lp;
   *part_g = p->part_g;
+  *lin = p->lin;
   return GNUTS_OK;
 }
 
@@ -547,11 +631,12 @@ void tc_destroy(TcPlan* p) {
   cudaFree(p->error);
   cudaFree(p->part_lp);
   cudaFree(p->part_g);
+  cudaFree(p->lin);
   delete p;
 }
 
 void tc_launch(const TcPlan* p, cudaStream_t stream) {
-  k_glm_tc<<<p->grid, NUM_THREADS, SMEM_BYTES, stream>>>(p->xmap, p->cmap, p->args);
+  k_glm_tc<<<p->grid, NUM_THREADS, SMEM_BYTES, stream>>>(p->xmap, p->args);
 }
 
 int tc_error(const TcPlan* p) {

@@ -50,6 +50,9 @@ struct DevModel {
   // y packed 32 rows per word
   const uint16_t* Xtc;
   const uint32_t* ybits;
+  // Xtc^T (y - 1/2) in FP64, XTC_LD entries: the linear part of the
+  // likelihood is B . xtc_ym for a coefficient row B in Xtc's column order
+  const double* xtc_ym;
   // varint: parameter order [beta, log sigma_y, log tau, alpha] (posterior
   // sets, so that the shared parameters sit in the same columns for every
   // posterior) and FP32 likelihood rows (FP64 sums across groups)

@@ -143,6 +143,24 @@ __global__ void k_derive_xtc(const uint16_t* Xb, size_t rows, int K, uint16_t* X
       Xtc[n * XTC_LD + k] = k < K ? Xb[n * K + k] : (k == K ? (uint16_t)0x3f80 : (uint16_t)0);
   }
 }
+// column k of Xtc^T (y - 1/2) in FP64, one block per column; fixed
+// per-thread row order and a fixed tree, so the result is reproducible
+__global__ void k_xtc_ym(const uint16_t* Xtc, const int* y, int rows, double* out) {
+  __shared__ double red[256];
+  const int k = blockIdx.x;
+  double s = 0;
+  for (int n = threadIdx.x; n < rows; n += blockDim.x) {
+    const float x = __uint_as_float((uint32_t)Xtc[(size_t)n * XTC_LD + k] << 16);
+    s += (double)x * (y[n] ? 0.5 : -0.5);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[k] = red[0];
+}
 // y packed 32 rows per word (words beyond the data are zero)
 __global__ void k_pack_y(const int* y, size_t rows, size_t words, uint32_t* out) {
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x) {
@@ -234,7 +252,22 @@ int upload(Model& m, std::string& err) {
   // every device entry point passes here: drop a stale non-sticky error left
   // by an earlier runtime call so that launch checks report this call's errors
   (void)cudaGetLastError();
-  if (m.device >= 0) return GNUTS_OK;
+  if (m.device >= 0) {
+    // the model's data lives on the device it was uploaded to: refuse a call
+    // made with another device current instead of launching on foreign pointers
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) {
+      err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+      return GNUTS_ERR_CUDA;
+    }
+    if (cur != m.device) {
+      err = "the model's data is on CUDA device " + std::to_string(m.device) + " but device " + std::to_string(cur) +
+            " is current; make device " + std::to_string(m.device) + " current for calls on this model";
+      return GNUTS_ERR_ARGUMENT;
+    }
+    return GNUTS_OK;
+  }
   int rc = ensure_device(err);
   if (rc) return rc;
   auto put = [&](const void* src, size_t bytes, void** dst) -> int {
@@ -271,6 +304,7 @@ int upload(Model& m, std::string& err) {
     if (tc) {
       if ((rc = dev_alloc(sizeof(uint16_t) * (size_t)h.N * XTC_LD, (void**)&d.Xtc))) return rc;
       if ((rc = dev_alloc(sizeof(uint32_t) * (((size_t)h.N + 31) / 32 + 4), (void**)&d.ybits))) return rc;
+      if ((rc = dev_alloc(sizeof(double) * XTC_LD, (void**)&d.xtc_ym))) return rc;
     }
     k_derive_x<<<std::min<size_t>(4096, (xn + 255) / 256), 256>>>(d.X, xn, const_cast<float*>(d.Xf),
                                                                   const_cast<uint16_t*>(d.Xb));
@@ -281,6 +315,7 @@ int upload(Model& m, std::string& err) {
       const size_t words = (rows + 31) / 32 + 4;
       k_pack_y<<<std::min<size_t>(4096, (words + 255) / 256), 256>>>(d.yi, rows, words,
                                                                      const_cast<uint32_t*>(d.ybits));
+      k_xtc_ym<<<XTC_LD, 256>>>(d.Xtc, d.yi, h.N, const_cast<double*>(d.xtc_ym));
     }
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { err = std::string("deriving X copies: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
@@ -377,7 +412,7 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   G.K = M.K;
   G.done_count = done_count;
   if (prec == GNUTS_PRECISION_MIXED && tc_supported(M)) {
-    int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g32, err);
+    int st = tc_create(M, C, done_count, &gs.plan, &G.coef_bf, &G.S, &G.part_lp, &G.part_g32, &G.lin, err);
     if (st) return st;
     G.tc = gs.plan;
     G.Cpad = (C + 127) / 128 * 128;

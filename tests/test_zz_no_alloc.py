@@ -26,21 +26,24 @@ def _noalloc(model, q_dev, lp_dev, g_dev, n, jacobian=True):
                                            ctypes.c_void_p(lp_dev.data_ptr()), ctypes.c_void_p(g_dev.data_ptr()))
 
 
-@pytest.mark.parametrize("mid,data,n", [
-    ("logistic", workloads.logistic(seed=31, N=6000, D=40), 48),
-    ("horseshoe", workloads.horseshoe(seed=32, N=5000, D=30, n_nonzero=3), 64),
+@pytest.mark.parametrize("mid,data,n,jacobian", [
+    ("logistic", workloads.logistic(seed=31, N=6000, D=40), 48, True),
+    ("horseshoe", workloads.horseshoe(seed=32, N=5000, D=30, n_nonzero=3), 64, True),
+    # the horseshoe's constrained scales carry a Jacobian that the finishing
+    # kernel removes again when it is off
+    ("horseshoe", workloads.horseshoe(seed=32, N=5000, D=30, n_nonzero=3), 64, False),
 ])
-def test_noalloc_matches_allocating_entry_point(mid, data, n):
+def test_noalloc_matches_allocating_entry_point(mid, data, n, jacobian):
     torch = pytest.importorskip("torch")
     model = gn.Model(mid, data)
     rng = np.random.default_rng(7)
     q = rng.normal(0.0, 0.2, (n, model.dim))
-    lp_ref, g_ref = model.log_prob_grad(q)  # the allocating entry point (also uploads the data)
+    lp_ref, g_ref = model.log_prob_grad(q, jacobian=jacobian)  # the allocating entry point (also uploads the data)
     q_dev = torch.tensor(q, dtype=torch.float64, device="cuda")
     for call in range(2):
         lp_dev = torch.full((n,), float("nan"), dtype=torch.float64, device="cuda")
         g_dev = torch.full((n, model.dim), float("nan"), dtype=torch.float64, device="cuda")
-        rc = _noalloc(model, q_dev, lp_dev, g_dev, n)
+        rc = _noalloc(model, q_dev, lp_dev, g_dev, n, jacobian)
         assert rc == gnuts.GNUTS_OK, call
         lp, g = lp_dev.cpu().numpy(), g_dev.cpu().numpy()
         np.testing.assert_allclose(lp, lp_ref, rtol=1e-10, atol=0)

@@ -221,6 +221,35 @@ __device__ __forceinline__ float rcpa(float x) {
   return y;
 }
 
+// Two FP32 lanes in one 64-bit register (element 0 in the low half) and the
+// packed f32x2 arithmetic of sm_100-class parts: one instruction per pair.
+// The epilogue does its FP32 work on pairs because scalar FP32 arithmetic at
+// full issue rate starves the single MMA-issuing thread of issue slots (it
+// shares a scheduler with four epilogue warps); the packed forms perform the
+// same IEEE operations in half the instructions.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2pack(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2unpack(f2 v, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+__device__ __forceinline__ f2 f2add(f2 a, f2 b) {
+  f2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 f2mul(f2 a, f2 b) {
+  f2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c) {
+  f2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&v);
@@ -387,8 +416,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int et = threadIdx.x - 64;    // 0 .. 511
     float* ys = (float*)(smem + OFF_Y);
     // stage y - 1/2 of this row split as floats (read back as warp-wide
-    // broadcasts).  Thread et writes float4 number f = et + 512 k (rows 4f ..
-    // 4f + 3, from packed word f / 8: row_begin is a multiple of 128); the
+    // broadcasts), each group of four rows in the order (0, 2, 1, 3) that the
+    // epilogue pairs them in.  Thread et writes float4 number f = et + 512 k
+    // (rows 4f .. 4f + 3, from packed word f / 8: row_begin is a multiple of 128); the
     // loads of a thread's four float4 are issued together.  Rows past the data
     // have zero bits (the packed words are zero-padded), i.e. y - 1/2 = -1/2.
     {
@@ -406,8 +436,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           const int f = f0 + k * 32 * EPI_WARPS;
           const uint32_t bb = w[k] >> (4 * (f & 7));
           if (f < nf)
-            reinterpret_cast<float4*>(ys)[f] = make_float4((bb & 1u) ? 0.5f : -0.5f, (bb & 2u) ? 0.5f : -0.5f,
-                                                           (bb & 4u) ? 0.5f : -0.5f, (bb & 8u) ? 0.5f : -0.5f);
+            reinterpret_cast<float4*>(ys)[f] = make_float4((bb & 1u) ? 0.5f : -0.5f, (bb & 4u) ? 0.5f : -0.5f,
+                                                           (bb & 2u) ? 0.5f : -0.5f, (bb & 8u) ? 0.5f : -0.5f);
         }
       }
     }
@@ -436,34 +466,40 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = j < nvalid ? v[j] : 0.f;
       }
-      // products of (1 + e) over alternate quads (each at most 2^16), |h| sums
-      float pr0 = 1.f, pr1 = 1.f, sa0 = 0.f, sa1 = 0.f;
+      // per quad of rows 0..3, pairs A = (0, 2) and B = (1, 3); products of
+      // (1 + e) over alternate quads (each at most 2^16); sums of
+      // t = -log2(e) |h| in pairs (|h| = -t ln 2)
+      const f2 ONE2 = f2pack(1.f, 1.f), MHALF2 = f2pack(-0.5f, -0.5f);
+      float pr0 = 1.f, pr1 = 1.f;
+      f2 tsA = f2pack(0.f, 0.f), tsB = f2pack(0.f, 0.f);
       uint32_t hi[16];
 #pragma unroll
       for (int j4 = 0; j4 < 8; ++j4) {
-        const float4 yv = y4[j4];  // y - 1/2
+        const float4 yv = y4[j4];  // y - 1/2 of rows 0, 2, 1, 3
         const float x0 = v[4 * j4], x1 = v[4 * j4 + 1], x2 = v[4 * j4 + 2], x3 = v[4 * j4 + 3];
-        const float d0 = 1.f + ex2a(-1.4426950408889634f * fabsf(x0));
-        const float d1 = 1.f + ex2a(-1.4426950408889634f * fabsf(x1));
-        const float d2 = 1.f + ex2a(-1.4426950408889634f * fabsf(x2));
-        const float d3 = 1.f + ex2a(-1.4426950408889634f * fabsf(x3));
-        const float p01 = d0 * d1, p23 = d2 * d3;
+        const float t0 = -1.4426950408889634f * fabsf(x0), t1 = -1.4426950408889634f * fabsf(x1);
+        const float t2 = -1.4426950408889634f * fabsf(x2), t3 = -1.4426950408889634f * fabsf(x3);
+        const f2 tA = f2pack(t0, t2), tB = f2pack(t1, t3);
+        const f2 dA = f2add(f2pack(ex2a(t0), ex2a(t2)), ONE2);  // (d0, d2), d = 1 + e
+        const f2 dB = f2add(f2pack(ex2a(t1), ex2a(t3)), ONE2);  // (d1, d3)
+        const f2 P = f2mul(dA, dB);                              // (d0 d1, d2 d3)
+        float p01, p23;
+        f2unpack(P, p01, p23);
         const float pq = p01 * p23;
         const float rq = rcpa(pq);
-        const float r01 = p23 * rq, r23 = p01 * rq;  // 1 / (d0 d1), 1 / (d2 d3)
+        const f2 S = f2mul(f2pack(p23, p01), f2pack(rq, rq));   // (1 / (d0 d1), 1 / (d2 d3))
         // inv_logit(|h|) - 1/2 = 1/d - 1/2, and
         // y - inv_logit(h) = (y - 1/2) - sign(h) (inv_logit(|h|) - 1/2)
-        const float w0 = fmaf(d1, r01, -0.5f), w1 = fmaf(d0, r01, -0.5f);
-        const float w2 = fmaf(d3, r23, -0.5f), w3 = fmaf(d2, r23, -0.5f);
-        const float R0 = yv.x - copysignf(w0, x0), R1 = yv.y - copysignf(w1, x1);
-        const float R2 = yv.z - copysignf(w2, x2), R3 = yv.w - copysignf(w3, x3);
-        if (j4 & 1) {
-          pr1 *= pq;
-          sa1 += (fabsf(x0) + fabsf(x1)) + (fabsf(x2) + fabsf(x3));
-        } else {
-          pr0 *= pq;
-          sa0 += (fabsf(x0) + fabsf(x1)) + (fabsf(x2) + fabsf(x3));
-        }
+        float w0, w1, w2, w3;
+        f2unpack(f2fma(dB, S, MHALF2), w0, w2);
+        f2unpack(f2fma(dA, S, MHALF2), w1, w3);
+        float R0, R1, R2, R3;
+        f2unpack(f2add(f2pack(yv.x, yv.y), f2pack(copysignf(w0, -x0), copysignf(w2, -x2))), R0, R2);
+        f2unpack(f2add(f2pack(yv.z, yv.w), f2pack(copysignf(w1, -x1), copysignf(w3, -x3))), R1, R3);
+        if (j4 & 1) pr1 *= pq;
+        else pr0 *= pq;
+        tsA = f2add(tsA, tA);
+        tsB = f2add(tsB, tB);
         hi[2 * j4] = pack_bf16(R0, R1);
         hi[2 * j4 + 1] = pack_bf16(R2, R3);
       }
@@ -472,7 +508,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         // the data contributed exactly one factor 2 and nothing to |h|
         float l2 = lg2a(pr0 * pr1);
         if (nvalid < 32) l2 -= (float)(32 - max(nvalid, 0));
-        const float yk = -fmaf(l2, 0.69314718055994531f, 0.5f * (sa0 + sa1)) - lp_comp;
+        float ta0, ta1, tb0, tb1;
+        f2unpack(tsA, ta0, ta1);
+        f2unpack(tsB, tb0, tb1);
+        const float tsum = (ta0 + ta1) + (tb0 + tb1);  // -log2(e) sum |h|
+        const float yk = -fmaf(l2, 0.69314718055994531f, -0.34657359027997264f * tsum) - lp_comp;
         const float tk = lp_acc + yk;
         lp_comp = (tk - lp_acc) - yk;
         lp_acc = tk;

@@ -110,6 +110,10 @@ __device__ __forceinline__ double lse(double a, double b) {
   return m + log1p(exp(-fabs(a - b)));
 }
 
+// MET >= 0 fixes the metric at compile time (0 diag_e, 1 dense_e, 2 unit_e):
+// a kernel instantiated per metric carries only that metric's code on its
+// hot path; MET = -1 reads it from the run's parameters.
+template <int MET = -1>
 struct Chain {
   const Params& P;
   const Bufs& B;
@@ -139,6 +143,7 @@ struct Chain {
     wm = b.wm + o;
     wm2 = b.wm2 + mo;
   }
+  __device__ __forceinline__ int metric() const { return MET >= 0 ? MET : P.metric; }
   __device__ double* rec(int r, int v) const {
     return B.rec + (((size_t)c * P.R + r) * 7 + v) * P.ld;
   }
@@ -162,7 +167,7 @@ struct Chain {
   // One launch loads the chain's working vectors into this warp's slice of
   // shared memory (independent loads, all in flight at once) and writes them
   // back at exit, so the state machine's dependent accesses stay on chip.
-  __device__ int cached_vectors() const { return P.metric == 1 ? NCACHE_VEC : NCACHE_VEC_DIAG; }
+  __device__ int cached_vectors() const { return metric() == 1 ? NCACHE_VEC : NCACHE_VEC_DIAG; }
   template <class F>
   __device__ void for_each_cached(F f) {
     double** v[NCACHE_VEC_DIAG] = {&Wq, &Wp, &Wg, &Fq, &Fp, &Fg, &Bq, &Bp, &Bg, &Sq,
@@ -267,19 +272,19 @@ struct Chain {
   }
   // out = minv * p  (p must be visible to the whole warp for dense)
   __device__ void dtau(double* out, const double* p) const {
-    if (P.metric != 1) {
+    if (metric() != 1) {
       for (int base = 0; base < D; base += 32 * VCW) {
         double vm[VCW], vp[VCW];
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
           vp[j] = d < D ? p[d] : 0.0;
-          vm[j] = d < D && P.metric == 0 ? minv[d] : 0.0;
+          vm[j] = d < D && metric() == 0 ? minv[d] : 0.0;
         }
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
           const int d = base + lane + 32 * j;
-          if (d < D) out[d] = P.metric == 0 ? vm[j] * vp[j] : vp[j];
+          if (d < D) out[d] = metric() == 0 ? vm[j] * vp[j] : vp[j];
         }
       }
     } else {
@@ -296,7 +301,7 @@ struct Chain {
 
   __device__ void sample_p(double* p) {
     const uint64_t n0 = s.rng_n;
-    if (P.metric == 1) {
+    if (metric() == 1) {
       for (int d = lane; d < D; d += 32) tmp[d] = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
       __syncwarp();
       // solve Lt p = z, back substitution over rows of Lt (Lt[i][k] = L[k][i])
@@ -312,7 +317,7 @@ struct Chain {
     } else {
       for (int d = lane; d < D; d += 32) {
         double z = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
-        p[d] = P.metric == 0 ? z / sqrt(minv[d]) : z;
+        p[d] = metric() == 0 ? z / sqrt(minv[d]) : z;
       }
     }
     s.rng_n = n0 + (uint64_t)((D + 1) / 2);
@@ -322,7 +327,7 @@ struct Chain {
 
   // W.p += e/2 g ; W.q += e * minv W.p   (gradient at W.q then requested)
   __device__ void begin_leapfrog(double e) {
-    if (P.metric == 1) {
+    if (metric() == 1) {
       for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
       dtau(tmp, Wp);
       for (int d = lane; d < D; d += 32) Wq[d] += e * tmp[d];
@@ -336,7 +341,7 @@ struct Chain {
           vp[j] = ok ? Wp[d] : 0.0;
           vg[j] = ok ? Wg[d] : 0.0;
           vq[j] = ok ? Wq[d] : 0.0;
-          vm[j] = ok && P.metric == 0 ? minv[d] : 0.0;
+          vm[j] = ok && metric() == 0 ? minv[d] : 0.0;
         }
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
@@ -344,7 +349,7 @@ struct Chain {
           if (d < D) {
             const double pn = vp[j] + 0.5 * e * vg[j];
             Wp[d] = pn;
-            Wq[d] = vq[j] + e * (P.metric == 0 ? vm[j] * pn : pn);
+            Wq[d] = vq[j] + e * (metric() == 0 ? vm[j] * pn : pn);
           }
         }
       }
@@ -473,8 +478,8 @@ struct Chain {
       if (P.adapt) s.nom_eps = exp(s.da_xbar);  // complete_adaptation
       s.t_warm = globaltimer();
       if (lane == 0) B.out_eps[c] = s.nom_eps;
-      const size_t msz = P.metric == 1 ? (size_t)D * D : (size_t)P.D;
-      if (P.metric == 1) {
+      const size_t msz = metric() == 1 ? (size_t)D * D : (size_t)P.D;
+      if (metric() == 1) {
         for (int i = 0; i < D; ++i)
           for (int j = lane; j < D; j += 32) B.out_minv[(size_t)c * msz + (size_t)i * D + j] = minv[(size_t)i * P.ld + j];
       } else {
@@ -618,7 +623,7 @@ struct Chain {
     // p_sharp = minv p is formed in registers and stored to both ends of the
     // new leaf record (the dense metric needs the warp-wide product first)
     double kin = 0;
-    if (P.metric == 1) {
+    if (metric() == 1) {
       dtau(tmp, Wp);
       for (int d = lane; d < D; d += 32) kin += Wp[d] * tmp[d];
       for (int d = lane; d < D; d += 32) {
@@ -636,7 +641,7 @@ struct Chain {
           const int d = base + lane + 32 * j;
           const bool ok = d < D;
           vp[j] = ok ? Wp[d] : 0.0;
-          vm[j] = ok && P.metric == 0 ? minv[d] : 0.0;
+          vm[j] = ok && metric() == 0 ? minv[d] : 0.0;
           vq[j] = ok ? Wq[d] : 0.0;
           vg[j] = ok ? Wg[d] : 0.0;
         }
@@ -645,7 +650,7 @@ struct Chain {
           const int d = base + lane + 32 * j;
           if (d < D) {
             const double p = vp[j];
-            const double ps = P.metric == 0 ? vm[j] * p : p;
+            const double ps = metric() == 0 ? vm[j] * p : p;
             kin += p * ps;
             pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
             rq[d] = vq[j]; rg[d] = vg[j];
@@ -790,7 +795,7 @@ struct Chain {
       double xe = pow(s.da_counter, -P.kappa);
       s.da_xbar = (1.0 - xe) * s.da_xbar + xe * x;
       s.nom_eps = exp(x);
-      if (P.metric != 2) {
+      if (metric() != 2) {
         if (learn_metric()) {
           if (s.phase == PH_ERROR) return false;
           return begin_init_stepsize(1);
@@ -820,7 +825,7 @@ struct Chain {
     }
     const double n = s.wf_n;
     bool ok = true;
-    if (P.metric == 1) {
+    if (metric() == 1) {
       for (int i = 0; i < D; ++i)
         for (int j = lane; j < D; j += 32) {
           double v = wm2[(size_t)i * P.ld + j] / (n - 1.0);
@@ -838,11 +843,11 @@ struct Chain {
     }
     __syncwarp();
     if (!wall(ok)) { fail(CE_METRIC); return true; }
-    if (P.metric == 1 && !cholesky()) { fail(CE_NOT_PD); return true; }
+    if (metric() == 1 && !cholesky()) { fail(CE_NOT_PD); return true; }
     // restart the estimator
     s.wf_n = 0;
     for (int d = lane; d < D; d += 32) wm[d] = 0;
-    if (P.metric == 1) {
+    if (metric() == 1) {
       for (int i = 0; i < D; ++i)
         for (int j = lane; j < D; j += 32) wm2[(size_t)i * P.ld + j] = 0;
     } else {
@@ -860,10 +865,10 @@ struct Chain {
       double q = Sq[d];
       double delta = q - wm[d];
       wm[d] += delta / n;
-      if (P.metric == 1) tmp[d] = delta;
+      if (metric() == 1) tmp[d] = delta;
       else wm2[d] += (q - wm[d]) * delta;
     }
-    if (P.metric == 1) {
+    if (metric() == 1) {
       __syncwarp();
       for (int i = 0; i < D; ++i) {
         double a = Sq[i] - wm[i];

@@ -98,14 +98,16 @@ __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, R
   if (lane == 0) B.sc[warp] = s;
 }
 
-// Round mode: advance every live chain by one gradient.
+// Round mode: advance every live chain by one gradient.  Instantiated per
+// metric (MET), so the diag_e kernel's hot path carries no dense-metric code.
+template <int MET>
 __global__ void __launch_bounds__(128) k_advance(Params P, Bufs B, DevModel M, GradOut G) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= P.C) return;
   Scal s = B.sc[warp];
   if (s.phase >= PH_DONE) return;
-  Chain ch(P, B, M, s, warp, lane);
+  Chain<MET> ch(P, B, M, s, warp, lane);
   extern __shared__ double gn_cache[];
   if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
   // gather this chain's gradient from the batched kernel's partial sums
@@ -116,6 +118,13 @@ __global__ void __launch_bounds__(128) k_advance(Params P, Bufs B, DevModel M, G
   if (P.cache) ch.cache_detach();
   __syncwarp();
   if (lane == 0) B.sc[warp] = s;
+}
+
+static void launch_advance(int blocks, int threads, size_t smem, cudaStream_t st, const Params& P, const Bufs& B,
+                           const DevModel& M, const GradOut& G) {
+  if (P.metric == 0) k_advance<0><<<blocks, threads, smem, st>>>(P, B, M, G);
+  else if (P.metric == 1) k_advance<1><<<blocks, threads, smem, st>>>(P, B, M, G);
+  else k_advance<2><<<blocks, threads, smem, st>>>(P, B, M, G);
 }
 
 __global__ void k_log_prob_grad(DevModel M, int n, const double* q, int jac, double* lp, double* g) {
@@ -519,7 +528,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   int glm_rc = GNUTS_OK;
   for (int r = 0; r < ROUNDS; ++r) {
     glm_rc |= launch_glm(G, M, stream);
-    k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
+    launch_advance(blocks, threads, cache_bytes(P), stream, P, B, M, G);
   }
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
   if (glm_rc) {
@@ -553,7 +562,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
         return GNUTS_ERR_CUDA;
       }
       GN_CUDA(cudaEventRecord(tev[1], stream));
-      k_advance<<<blocks, threads, cache_bytes(P), stream>>>(P, B, M, G);
+      launch_advance(blocks, threads, cache_bytes(P), stream, P, B, M, G);
       GN_CUDA(cudaEventRecord(tev[2], stream));
       rounds += 1;
       launches += 2;
@@ -679,7 +688,9 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     P.cache = bytes <= 160 * 1024 && !rounds;
     if (P.cache) {
       GN_CUDA(fused_set_smem(m.dev.kind, (int)bytes));
-      GN_CUDA(cudaFuncSetAttribute(k_advance, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      GN_CUDA(cudaFuncSetAttribute(k_advance<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      GN_CUDA(cudaFuncSetAttribute(k_advance<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      GN_CUDA(cudaFuncSetAttribute(k_advance<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     } else if (!rounds && (size_t)P.cache_stride * sizeof(double) <= 200 * 1024) {
       // large chains: the cache can still hold one or two chains per CTA
       // (the fused-mode autotuner decides whether that pays)

@@ -8,7 +8,14 @@ min bulk-ESS/s is defined).  Reported:
   e2e         the same metric through the C ABI with host buffers: model
               creation (X and y copied host -> device), sampling, draws copied
               device -> host, all inside the timed region
-  min_bulk_ess_per_s, rhat_max   from the draws of each run
+  min_bulk_ess_per_s, rhat_max   from the draws of the last run; the ESS is
+              divided by that run's wall time (warmup + sampling, host calls
+              included), as the metric is defined
+  precision_vs_fp64   the mixed-precision gradient against the FP64 one at 64
+              posterior draws of the run: largest relative lp error and largest
+              gradient error relative to the largest component
+  config2_fp64  the same workload on the FP64 CUDA-core gradient (a bounded
+              run: 64 chains, 150 warmup + 150 draws)
   roofline    the tcgen05 gradient kernel: algorithmic 4*N*D flops per chain
               per round over its CUDA-event duration, against the measured
               sustained bf16 peak
@@ -150,10 +157,14 @@ def cpu_sample(data, seconds=15.0, threads=None):
     per_iter = probe / 2.0
     iters = int(max(2, min(400, seconds / max(per_iter, 1e-6))))
     t = time.time()
-    _, _, _, ng = om.run_chains(threads, threads=threads, inits=w, inv_metric=var, num_samples=iters, **kw)
+    dr, _, _, ng = om.run_chains(threads, threads=threads, inits=w, inv_metric=var, num_samples=iters, **kw)
     wall = time.time() - t
+    ess = min(oracle.ess_bulk(np.ascontiguousarray(dr[:, :, j])) for j in range(7, dr.shape[2]))
     return {"value": float(ng.sum() / wall), "unit": "grad-evals/s", "cores": threads, "kind": "port",
-            "wall_s": wall,
+            "wall_s": wall, "min_bulk_ess_per_s": float(ess / wall),
+            "min_bulk_ess_note": "min bulk ESS over the 101 parameters of these draws / wall; the chains start "
+                                 "at the posterior mode with the Laplace metric and skip warmup, which favours "
+                                 "the CPU",
             "sample": "%d chains x %d transitions (adaptation off, started at the posterior mode, Laplace diag "
                       "metric, step 0.7) of the same workload, FP64, %d host threads; %.1f s" %
                       (threads, iters, threads, wall)}
@@ -176,7 +187,8 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
             "config": config(args),
             "cpu_baseline": {"value": v, "unit": "grad-evals/s", "cores": res[-1]["cores"], "kind": "port",
-                             "sample": res[-1]["sample"]},
+                             "sample": res[-1]["sample"], "min_bulk_ess_per_s": res[-1]["min_bulk_ess_per_s"],
+                             "min_bulk_ess_note": res[-1]["min_bulk_ess_note"]},
             "e2e": {"value": v, "unit": "grad-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's own implementation (stan submodule) is absent from the reference tree; "
                     "the CPU oracle restating it times the CPU path; a step is one bounded sample of the "
@@ -211,6 +223,37 @@ def _min_ess_rhat(draws, cols_per_chain_group=None, per_group=None):
             sm += g
             c0 += n
     return float(min(s["ess_bulk"] for s in sm)), float(max(s["rhat"] for s in sm))
+
+
+def precision_vs_fp64(model, draws, n=64):
+    """Mixed-precision gradient against the FP64 one at n posterior draws
+    (the last draw of the first n chains): largest relative lp error and
+    largest gradient error relative to the largest gradient component."""
+    import cmdstan_gb300 as gn
+    q = np.array([model.unconstrain(np.ascontiguousarray(c)) for c in draws[:n, -1, 7:]])
+    lp64, g64 = model.log_prob_grad(q)
+    lpm, gm = model.log_prob_grad(q, precision=gn.PRECISION_MIXED)
+    return {"points": int(q.shape[0]), "where": "posterior draws of the run",
+            "lp_rel_err_max": float(np.max(np.abs(lpm - lp64) / np.abs(lp64))),
+            "grad_err_max_rel_to_max_component": float(np.max(np.max(np.abs(gm - g64), axis=1) /
+                                                              np.max(np.abs(g64), axis=1)))}
+
+
+def bench_fp64_arm(model, chains=64, warmup=150, samples=150):
+    """The logistic workload on the FP64 CUDA-core gradient (k_glm_simt<double>),
+    a bounded run: grad-evals/s over device time, min bulk-ESS/s over wall time."""
+    t0 = time.perf_counter()
+    fit = model.sample(num_chains=chains, num_warmup=warmup, num_samples=samples, seed=7, refresh=0)
+    wall = time.perf_counter() - t0
+    ess, rhat = _min_ess_rhat(fit.draws)
+    dev_s = fit.timing["device_ms"] / 1e3
+    g_us = float(fit.timing["grad_kernel_us"])
+    return {"workload": "logistic regression N=100000 x D=100, %d chains, %d warmup + %d draws (bounded sample), "
+                        "FP64 gradient on CUDA cores" % (chains, warmup, samples),
+            "grad_evals_per_s": float(fit.n_leapfrog.sum() / dev_s), "min_bulk_ess_per_s": ess / wall,
+            "min_bulk_ess": ess, "rhat_max": rhat, "wall_s": wall,
+            "kernels_us": {"k_glm_simt_fp64": g_us, "k_advance": float(fit.timing["advance_kernel_us"])},
+            "fp64_tflops_achieved": 4.0 * N_ROWS * N_PRED * chains / (g_us * 1e-6) / 1e12}
 
 
 def bench_varint_set(peaks):
@@ -305,6 +348,7 @@ def bench_horseshoe(peaks, chains=256):
     N, K = d["X"].shape
     fit = m.sample(num_chains=chains, num_warmup=30, num_samples=10, seed=3, precision=gn.PRECISION_MIXED,
                    refresh=0)
+    prec = precision_vs_fp64(m, fit.draws, n=16)
     tm = fit.timing
     dev_s = float(tm["device_ms"]) / 1e3
     grads = float(fit.n_leapfrog.sum())
@@ -324,6 +368,7 @@ def bench_horseshoe(peaks, chains=256):
                         "(bounded sample), mixed precision" % chains,
             "grad_evals_per_s": grads / dev_s, "device_s": dev_s, "leapfrogs": grads,
             "kernels_us": {"wide_gradient": g_us, "k_advance": float(tm["advance_kernel_us"])},
+            "precision_vs_fp64": prec,
             "roofline": {"bound": "tensor", "achieved": flops / (g_us * 1e-6) / 1e12,
                          "peak": peaks.get("bf16_tflops_sustained", 1709.0), "unit": "TFLOP/s",
                          "frac": flops / (g_us * 1e-6) / 1e12 / peaks.get("bf16_tflops_sustained", 1709.0),
@@ -477,7 +522,8 @@ def main():
     t_sum = time.perf_counter() - t_sum
     ess_min = float(min(s["ess_bulk"] for s in sm))
     rhat_max = float(max(s["rhat"] for s in sm))
-    step_s = last.timing["device_ms"] / 1e3
+    step_wall_s = times[-1] / 1e3  # the last run's wall time: warmup + sampling
+    prec = precision_vs_fp64(model, last.draws)
     grad_us = float(np.mean([f.timing["grad_kernel_us"] for f in fits]))
     adv_us = float(np.mean([f.timing["advance_kernel_us"] for f in fits]))
     flops = 4.0 * N_ROWS * N_PRED * N_CHAINS
@@ -504,7 +550,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": wall_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2/fp32/fp64",
         "data": "synthetic (seeded PCG64, X rounded to bf16)", "config": config(args),
-        "min_bulk_ess_per_s": ess_min / step_s, "min_bulk_ess": ess_min, "rhat_max": rhat_max,
+        "min_bulk_ess_per_s": ess_min / step_wall_s, "min_bulk_ess": ess_min, "rhat_max": rhat_max,
+        "min_bulk_ess_per_s_denominator": "wall time of the run (warmup + sampling)",
+        "precision_vs_fp64": prec,
         "sampler_device_s_per_step": dev_ms / 1e3 / args.steps,
         "leapfrogs_per_step": lf / args.steps,
         "kernels_us": {"k_glm_tc": grad_us, "k_advance": adv_us},
@@ -512,7 +560,7 @@ def main():
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": "%s bf16 sustained" % peak_kind,
                      "note": "algorithmic 4*N*D flops per chain-gradient x 1024 chains per launch; the BF16 "
-                             "hi/lo split executes twice that on the tensor pipe"},
+                             "hi/lo split executes 1.5x that on the tensor pipe (K padded to 112)"},
         "e2e": {"value": e2e_value, "unit": "grad-evals/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "s_per_step": float(np.mean(e2e_times))},
         "gpu_launches": launches, "clocks": clocks,
@@ -522,7 +570,8 @@ def main():
     if rank == 0:
         if not args.no_extra:
             extra = {}
-            for name, fn in (("bernoulli", bench_bernoulli), ("varint_set_512x4", lambda: bench_varint_set(peaks)),
+            for name, fn in (("config2_fp64", lambda: bench_fp64_arm(model)), ("bernoulli", bench_bernoulli),
+                             ("varint_set_512x4", lambda: bench_varint_set(peaks)),
                              ("hier_64_learned_vs_plain", lambda: bench_learned("hier")),
                              ("funnel_100d_learned_vs_plain", lambda: bench_learned("funnel")),
                              ("horseshoe_2003d", lambda: bench_horseshoe(peaks))):

@@ -4,6 +4,7 @@ Compiles in-tree with nvcc / g++ directly (no cmake), in parallel, and only
 what changed.  Outputs:
     cmdstan_gb300/_lib/libgnuts.so     the product (C ABI of include/gnuts.h)
     cmdstan_gb300/_lib/gnuts-sample    CmdStan-compatible command line
+    cmdstan_gb300/_lib/gnuts-diagnose  the diagnose tool over Stan CSV files
     oracle/_build/liboracle.so         CPU oracle (test infrastructure)
 """
 import concurrent.futures as cf
@@ -29,7 +30,7 @@ CU_SOURCES = ["sampler.cu", "fused.cu", "grad_tc.cu", "grad_wide.cu", "noalloc.c
 # compiled once per model kind (-DGNUTS_KIND=k, k = 0..N_KINDS-1)
 CU_KIND_SOURCES = ["fused_kind.cu", "flow_tc_kind.cu"]
 N_KINDS = 7
-CPP_SOURCES = ["abi.cpp", "summary.cpp", "learned.cpp"]
+CPP_SOURCES = ["abi.cpp", "summary.cpp", "learned.cpp", "diagnose.cpp"]
 
 
 def _nvcc():
@@ -108,6 +109,10 @@ def build(verbose=False, jobs=None):
     if os.path.exists(cli_src) and _newer(exe, cli_deps + [so, os.path.join(INC, "gnuts.h")]):
         _run(["g++"] + CXX_FLAGS + ["-pthread", "-I" + CLI, cli_src, "-o", exe, "-L" + LIB, "-lgnuts",
                                     "-Wl,-rpath,$ORIGIN"])
+    diag_src = os.path.join(CLI, "gnuts_diagnose.cpp")
+    diag_exe = os.path.join(LIB, "gnuts-diagnose")
+    if os.path.exists(diag_src) and _newer(diag_exe, [diag_src, so, os.path.join(INC, "gnuts.h")]):
+        _run(["g++"] + CXX_FLAGS + [diag_src, "-o", diag_exe, "-L" + LIB, "-lgnuts", "-Wl,-rpath,$ORIGIN"])
     return so
 
 

@@ -37,6 +37,7 @@ EXPORTS = [
     "gnuts_flow_log_prob_grad", "gnuts_flow_log_prob_grad_tc", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
     "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt", "gnuts_train_args_default",
     "gnuts_summary_columns_gpu",
+    "gnuts_diagnose",
 ]
 SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
 
@@ -77,6 +78,31 @@ def summary_columns(draws, cols, probs=(0.05, 0.5, 0.95), threads=0, gpu=False):
     else:
         _check(lib.gnuts_summary_columns(_dp(d), C, n, len(cols), n * K, K, ci, _dp(p), len(p), threads, _dp(out)))
     return [_summary_dict(o, probs) for o in out]
+
+
+class Diagnosis(ctypes.Structure):
+    _fields_ = [("n_treedepth_max", ctypes.c_long), ("n_divergent", ctypes.c_long), ("e_bfmi", ctypes.c_double),
+                ("n_low_ess", ctypes.c_int), ("n_high_rhat", ctypes.c_int), ("has_problems", ctypes.c_int)]
+
+
+def diagnose(draws, names, max_depth=10, gpu=False, threads=0):
+    """CmdStan diagnose checks of a [chains, draws, columns] array whose
+    columns are named by `names` (Stan CSV order: the seven sampler columns,
+    then the parameters).  Returns (report text, dict of the counts)."""
+    lib = load()
+    d = np.ascontiguousarray(draws, dtype=np.float64)
+    C, n, K = d.shape
+    names = list(names)
+    col = lambda nm: names.index(nm) if nm in names else -1
+    pcols = [i for i, nm in enumerate(names) if "__" not in nm]
+    ci = np.ascontiguousarray(pcols, dtype=np.int32)
+    pn = "\n".join(names[i] for i in pcols).encode()
+    buf = ctypes.create_string_buffer(1 << 16 if len(pn) < 1 << 14 else 4 * len(pn) + (1 << 16))
+    res = Diagnosis()
+    _check(lib.gnuts_diagnose(_dp(d), C, n, n * K, K, col("treedepth__"), col("divergent__"), col("energy__"),
+                              ci.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(pcols), pn, int(max_depth),
+                              int(bool(gpu)), int(threads), buf, len(buf), ctypes.byref(res)))
+    return buf.value.decode(), {f: getattr(res, f) for f, _ in Diagnosis._fields_}
 
 
 class GnutsError(RuntimeError):
@@ -184,6 +210,8 @@ def load():
     lib.gnuts_summary.argtypes = [dp, ip, ip, i64, i64, dp, ip, dp]
     lib.gnuts_summary_columns.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, ip, dp]
     lib.gnuts_summary_columns_gpu.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, dp]
+    lib.gnuts_diagnose.argtypes = [dp, ip, ip, i64, i64, ip, ip, ip, ctypes.POINTER(ip), ip, ctypes.c_char_p, ip, ip,
+                                   ip, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p]
     lib.gnuts_flow_create.argtypes = [ip, ip, ip, ctypes.c_double, ctypes.POINTER(vp)]
     lib.gnuts_flow_destroy.argtypes = [vp]
     lib.gnuts_flow_destroy.restype = None

@@ -187,6 +187,29 @@ int gnuts_summary_columns_gpu(const double* draws, int n_chains, int n_iter, int
                               int64_t stride_iter, const int* cols, const double* probs, int n_probs,
                               double* out);
 
+/* Diagnostic checks of a run (CmdStan's bin/diagnose, src/cmdstan/diagnose.cpp:84-221):
+ * transitions at the maximum tree depth, divergences, E-BFMI < 0.3 (energy__
+ * over all chains' draws taken chain after chain), parameters with
+ * min(bulk, tail) ESS per draw < 0.001 and with max(bulk, tail) R-hat >
+ * 1.01499 (diagnose.cpp:12).  draws[c * stride_chain + i * stride_iter + col];
+ * a column index < 0 skips that check; param_names is '\n'-separated, in
+ * Stan CSV form ("mu.1" is reported as "mu[1]", as the CSV reader does).  The
+ * ESS / R-hat statistics run on host threads (use_gpu = 0) or on the GPU.
+ * report receives the reference's report text (NUL-terminated; an argument
+ * error if report_cap is too small). */
+typedef struct {
+  long n_treedepth_max;  /* transitions with treedepth__ >= max_depth */
+  long n_divergent;
+  double e_bfmi;         /* NaN without an energy column */
+  int n_low_ess;         /* parameters below 0.001 effective draws per transition */
+  int n_high_rhat;       /* parameters with R-hat above 1.01499 */
+  int has_problems;
+} gnuts_diagnosis;
+int gnuts_diagnose(const double* draws, int n_chains, int n_iter, int64_t stride_chain, int64_t stride_iter,
+                   int treedepth_col, int divergent_col, int energy_col, const int* param_cols, int n_params,
+                   const char* param_names, int max_depth, int use_gpu, int n_threads, char* report,
+                   size_t report_cap, gnuts_diagnosis* result);
+
 /* Allocation-free gradient for callers that cannot allocate device memory.
  * No counterpart in the reference: CmdStan computes gradients on the host.
  * It exists for callers that run where cudaMalloc is not allowed -- code

@@ -10,11 +10,21 @@ elapsed-time trailer).  The expected summary numbers are
 the literal goldens of src/test/interface/stansummary_test.cpp (:481-495,
 :622-637) and are written into the tests themselves.
 
-Usage: python tests/golden/make_golden.py /root/reference
+It also writes the fixtures of the diagnose tool's tests
+(src/test/interface/diagnose_test.cpp:11-98): for each case the sampler
+columns and parameter draws of its example CSV files as a compressed array
+(diag_<case>.npz: draws [chains, iterations, columns] in float32 -- the CSV
+values carry six significant digits -- column names, max_depth from the
+config block) and the expected report text (<case>.nom).
+
+Usage: python tests/golden/make_golden.py <path of the reference checkout>
 """
 import json
 import os
+import re
 import sys
+
+import numpy as np
 
 
 def parse_stan_csv(path):
@@ -63,5 +73,33 @@ def main(ref):
         print(stem, len(rows), "draws x", len(names), "columns")
 
 
+DIAGNOSE_CASES = [("corr_gauss", ["corr_gauss_output"]), ("corr_gauss_depth8", ["corr_gauss_output_depth8"]),
+                  ("corr_gauss_depth15", ["corr_gauss_output_depth15"]), ("eight_schools", ["eight_schools_output"]),
+                  ("mix", ["mix_output.1", "mix_output.2"])]
+
+
+def diagnose_fixtures(ref):
+    here = os.path.dirname(os.path.abspath(__file__))
+    ex = os.path.join(ref, "src/test/interface/example_output")
+    for case, stems in DIAGNOSE_CASES:
+        chains, names, max_depth = [], None, None
+        for stem in stems:
+            nm, rows, config, _, _ = parse_stan_csv(os.path.join(ex, stem + ".csv"))
+            for line in config:
+                m = re.search(r"max_depth = (\d+)", line)
+                if m:
+                    max_depth = int(m.group(1))
+            names = nm
+            chains.append(np.asarray(rows, dtype=np.float32))
+        np.savez_compressed(os.path.join(here, "diag_%s.npz" % case), draws=np.stack(chains),
+                            names=np.array(names), max_depth=np.int32(max_depth))
+        with open(os.path.join(ex, case + ".nom")) as f, open(os.path.join(here, case + ".nom"), "w") as g:
+            g.write(f.read())
+        print("diagnose", case, np.stack(chains).shape, "max_depth", max_depth)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])
+    diagnose_fixtures(sys.argv[1])

@@ -65,3 +65,37 @@ def test_gpu_summary_thousands_of_chains():
     for j in range(4):
         _close(dev[j], host[j], rtol=1e-8)
     print("host %.3f s, device %.3f s" % (th, tg))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["corr_gauss", "corr_gauss_depth8", "corr_gauss_depth15", "eight_schools", "mix"])
+def test_diagnose_gpu_matches_reference(case):
+    """gnuts_diagnose with the ESS / R-hat statistics on the GPU reproduces
+    the reference's diagnose reports (src/test/interface/diagnose_test.cpp)."""
+    import test_diagnose_cpu as tdc
+    draws, names, max_depth, nom = tdc.load_case(case)
+    text, _ = gnuts.diagnose(draws, names, max_depth=max_depth, gpu=True)
+    assert text == nom
+
+
+@pytest.mark.gpu
+def test_diagnose_gpu_many_chains_matches_host():
+    """2048 chains x 1000 draws x 12 parameters: the device statistics give the
+    host path's report and counts."""
+    import time
+    rng = np.random.default_rng(5)
+    C, n, P = 2048, 1000, 12
+    d = np.zeros((C, n, 7 + P))
+    d[:, :, 3] = rng.integers(1, 11, (C, n))
+    d[:, :, 5] = rng.random((C, n)) < 1e-4
+    d[:, :, 6] = rng.normal(size=(C, n))
+    d[:, :, 7:] = rng.normal(size=(C, n, P))
+    d[:512, :, 8] += 2.0  # a quarter of the chains off for one parameter: its R-hat is flagged
+    names = ["lp__", "accept_stat__", "stepsize__", "treedepth__", "n_leapfrog__", "divergent__", "energy__"] + \
+        ["b.%d" % (i + 1) for i in range(P)]
+    t = time.perf_counter()
+    tg, rg = gnuts.diagnose(d, names, gpu=True)
+    tgpu = time.perf_counter() - t
+    th, rh = gnuts.diagnose(d, names, gpu=False)
+    assert tg == th and rg["n_treedepth_max"] == rh["n_treedepth_max"] and rg["n_high_rhat"] == 1
+    print("diagnose of 2048 x 1000 x %d on the GPU: %.3f s" % (P, tgpu))

@@ -159,9 +159,11 @@ def cpu_sample(data, seconds=15.0, threads=None):
     t = time.time()
     dr, _, _, ng = om.run_chains(threads, threads=threads, inits=w, inv_metric=var, num_samples=iters, **kw)
     wall = time.time() - t
-    ess = min(oracle.ess_bulk(np.ascontiguousarray(dr[:, :, j])) for j in range(7, dr.shape[2]))
+    # the split-chain ESS needs a few draws per chain (a very short sample has none to give)
+    ess = (min(oracle.ess_bulk(np.ascontiguousarray(dr[:, :, j])) for j in range(7, dr.shape[2]))
+           if dr.shape[1] >= 8 else None)
     return {"value": float(ng.sum() / wall), "unit": "grad-evals/s", "cores": threads, "kind": "port",
-            "wall_s": wall, "min_bulk_ess_per_s": float(ess / wall),
+            "wall_s": wall, "min_bulk_ess_per_s": None if ess is None else float(ess / wall),
             "min_bulk_ess_note": "min bulk ESS over the 101 parameters of these draws / wall; the chains start "
                                  "at the posterior mode with the Laplace metric and skip warmup, which favours "
                                  "the CPU",

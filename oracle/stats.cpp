@@ -138,7 +138,8 @@ double ess_chains(const Chains& ch) {
   double rho_odd = 1.0 - (mean_var - mean_acov(1)) / var_plus;
   rho[0] = rho_even;
   rho[1] = rho_odd;
-  while (t < N - 5 && !std::isnan(rho_even + rho_odd) && (rho_even + rho_odd > 0)) {
+  // signed bound: with split chains of 4 draws, N - 5 is negative
+  while ((long)t < (long)N - 5 && !std::isnan(rho_even + rho_odd) && (rho_even + rho_odd > 0)) {
     t += 2;
     rho_even = 1.0 - (mean_var - mean_acov(t)) / var_plus;
     rho_odd = 1.0 - (mean_var - mean_acov(t + 1)) / var_plus;

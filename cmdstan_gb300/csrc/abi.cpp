@@ -552,7 +552,25 @@ int service(gnuts_model* mh, const gnuts_sample_args* a, const double* inits, co
 
 using namespace gnuts;
 
+namespace gnuts {
+RunHooks& run_hooks() {
+  thread_local RunHooks h;
+  return h;
+}
+}  // namespace gnuts
+
 extern "C" {
+
+void gnuts_set_interrupt(gnuts_interrupt_fn fn, void* ctx) {
+  gnuts::run_hooks().interrupt = fn;
+  gnuts::run_hooks().interrupt_ctx = ctx;
+}
+
+void gnuts_set_draw_sink(gnuts_draws_fn fn, void* ctx) {
+  gnuts::run_hooks().sink = fn;
+  gnuts::run_hooks().sink_ctx = ctx;
+}
+
 
 int gnuts_model_create(const char* model_id, const gnuts_var* vars, int n_vars, unsigned int seed, gnuts_model** out) {
   (void)seed;

@@ -1122,6 +1122,10 @@ int run_flow_fused(Model& m, const Flow& f, Params& P, const Bufs& B, double per
       ++launches;
       break;
     }
+    if (interrupt_requested()) {
+      err = "sampling interrupted by the caller's interrupt callback (gnuts_set_interrupt)";
+      return GNUTS_ERR_INTERRUPTED;
+    }
   }
   FL_CUDA(cudaEventRecord(e1));
   FL_CUDA(cudaEventSynchronize(e1));

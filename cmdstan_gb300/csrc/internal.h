@@ -106,6 +106,20 @@ struct RunConfig {
   double* q_last = nullptr;        // [C][D] final sampler-space position of every chain
 };
 
+// thread-local callbacks of the sampling services (gnuts_set_interrupt,
+// gnuts_set_draw_sink); sampler.cu and flow.cu poll them between launches
+struct RunHooks {
+  gnuts_interrupt_fn interrupt = nullptr;
+  void* interrupt_ctx = nullptr;
+  gnuts_draws_fn sink = nullptr;
+  void* sink_ctx = nullptr;
+};
+RunHooks& run_hooks();
+inline bool interrupt_requested() {
+  const RunHooks& h = run_hooks();
+  return h.interrupt && h.interrupt(h.interrupt_ctx) != 0;
+}
+
 // sampler.cu
 int run_nuts(Model& m, const gnuts_sample_args& a, const RunConfig& rc, const double* inits,
              const double* inv_metric, gnuts_output* out, gnuts_progress_fn progress, void* ctx,

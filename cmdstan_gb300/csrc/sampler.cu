@@ -495,13 +495,92 @@ int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, d
   return GNUTS_OK;
 }
 
+// Hands completed draw rows to the caller's sink (gnuts_set_draw_sink) while
+// the run proceeds.  Per-chain row counts are read back after launches that
+// have completed; once every chain has written rows [delivered, r), a block
+// of them (at most 64 MB) is copied with one strided copy on its own stream
+// -- those rows are final, so the copy runs beside the kernels -- and passed
+// to the sink.  finish() delivers the rest after the run.
+class DrawStreamer {
+ public:
+  DrawStreamer(const Params& P, const Bufs& B, bool enabled) : P_(P), B_(B) {
+    const RunHooks& h = run_hooks();
+    if (!enabled || !h.sink || P.n_saved == 0) return;
+    sink_ = h.sink;
+    ctx_ = h.sink_ctx;
+    const size_t row_bytes = (size_t)P.C * P.ncol * sizeof(double);
+    batch_ = (int)std::max<size_t>(1, std::min<size_t>((size_t)P.n_saved, (64u << 20) / row_bytes));
+  }
+  ~DrawStreamer() {
+    if (h_rows_) cudaFreeHost(h_rows_);
+    if (stage_) cudaFreeHost(stage_);
+    if (copy_) cudaStreamDestroy(copy_);
+  }
+  bool active() const { return sink_ != nullptr; }
+  // enqueue the read of every chain's row count into slot (0 or 1) on stream s
+  int request_rows(cudaStream_t s, int slot, std::string& err) {
+    if (!active()) return GNUTS_OK;
+    if (!h_rows_) {
+      GN_CUDA(cudaMallocHost(&h_rows_, sizeof(int) * 2 * P_.C));
+      std::fill(h_rows_, h_rows_ + 2 * P_.C, 0);
+    }
+    GN_CUDA(cudaMemcpy2DAsync(h_rows_ + slot * P_.C, sizeof(int), &B_.sc[0].row, sizeof(Scal), sizeof(int), P_.C,
+                              cudaMemcpyDeviceToHost, s));
+    return GNUTS_OK;
+  }
+  // the row counts in slot are complete (their launch has finished): deliver full blocks
+  int deliver(int slot, std::string& err) {
+    if (!active() || !h_rows_) return GNUTS_OK;
+    int min_row = P_.n_saved;
+    for (int c = 0; c < P_.C; ++c) min_row = std::min(min_row, h_rows_[slot * P_.C + c]);
+    while (min_row - delivered_ >= batch_) {
+      int st = send(batch_, err);
+      if (st) return st;
+    }
+    return GNUTS_OK;
+  }
+  int finish(std::string& err) {
+    while (active() && delivered_ < P_.n_saved) {
+      int st = send(std::min(batch_, P_.n_saved - delivered_), err);
+      if (st) return st;
+    }
+    return GNUTS_OK;
+  }
+
+ private:
+  int send(int k, std::string& err) {
+    const size_t rb = (size_t)P_.ncol * sizeof(double);
+    if (!stage_) {
+      GN_CUDA(cudaMallocHost(&stage_, rb * P_.C * batch_));
+      GN_CUDA(cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking));
+    }
+    GN_CUDA(cudaMemcpy2DAsync(stage_, rb * k, B_.draws + (size_t)delivered_ * P_.ncol, rb * P_.n_saved, rb * k,
+                              P_.C, cudaMemcpyDeviceToHost, copy_));
+    GN_CUDA(cudaStreamSynchronize(copy_));
+    sink_(ctx_, delivered_, k, stage_);
+    delivered_ += k;
+    return GNUTS_OK;
+  }
+  const Params& P_;
+  const Bufs& B_;
+  gnuts_draws_fn sink_ = nullptr;
+  void* ctx_ = nullptr;
+  int batch_ = 1, delivered_ = 0;
+  int* h_rows_ = nullptr;
+  double* stage_ = nullptr;
+  cudaStream_t copy_ = nullptr;
+};
+
+static const char* kInterrupted = "sampling interrupted by the caller's interrupt callback (gnuts_set_interrupt)";
+
 struct RunStats {
   double rounds = 0, grad_us = 0, advance_us = 0, device_ms = 0, launches = 0, reduce_us = 0;
   double chains_per_cta = 4;
 };
 
 static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double per_chain_max, int refresh,
-                      gnuts_progress_fn progress, void* ctx, RunStats& stats, std::string& err) {
+                      gnuts_progress_fn progress, void* ctx, DrawStreamer& streamer, RunStats& stats,
+                      std::string& err) {
   const DevModel& M = m.dev;
   if (M.K > 1024) { err = "batched gradient supports at most 1024 predictors"; return GNUTS_ERR_ARGUMENT; }
   GradSetup gs;
@@ -572,9 +651,16 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
       launches += 2 * ROUNDS;
     }
     GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    if ((st = streamer.request_rows(stream, b, err))) return st;
     GN_CUDA(cudaEventRecord(ev[b], stream));
     if (l > 0) {
       GN_CUDA(cudaEventSynchronize(ev[b ^ 1]));
+      if ((st = streamer.deliver(b ^ 1, err))) return st;
+      if (interrupt_requested()) {
+        cudaStreamSynchronize(stream);
+        err = kInterrupted;
+        return GNUTS_ERR_INTERRUPTED;
+      }
       if (timed_pending) {
         // the timed round was enqueued one step earlier and has completed
         float g_ms = 0, a_ms = 0;
@@ -773,6 +859,8 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
                                8.0 * 1200.0 + 200.0;
   int done = 0;
   RunStats stats;
+  // draw sink and interrupt callback of this thread (not for replayed transitions)
+  DrawStreamer streamer(P, B, !p0);
   if (rc.flow) {
     double fs[6] = {0, 0, 0, 0, 0, 4};
     st = run_flow_fused(m, *rc.flow, P, B, per_chain_max, fs, err);
@@ -790,7 +878,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       stats.launches += 1;
     }
   } else if (use_rounds(m) && !p0) {
-    st = run_rounds(m, P, B, a.precision, per_chain_max, a.refresh, progress, ctx, stats, err);
+    st = run_rounds(m, P, B, a.precision, per_chain_max, a.refresh, progress, ctx, streamer, stats, err);
     if (st) return st;
     GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
   } else {
@@ -848,6 +936,15 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       stats.rounds += 1;
       stats.launches += 1;
       GN_CUDA(cudaMemcpy(&done, B.done_count, sizeof(int), cudaMemcpyDeviceToHost));
+      if (streamer.active()) {
+        if ((st = streamer.request_rows(0, 0, err))) return st;
+        GN_CUDA(cudaStreamSynchronize(0));
+        if ((st = streamer.deliver(0, err))) return st;
+      }
+      if (!p0 && interrupt_requested()) {
+        err = kInterrupted;
+        return GNUTS_ERR_INTERRUPTED;
+      }
       if (progress && a.refresh > 0) {
         Scal s0;
         GN_CUDA(cudaMemcpy(&s0, B.sc, sizeof(Scal), cudaMemcpyDeviceToHost));
@@ -873,6 +970,7 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     return GNUTS_ERR_TIMEOUT;
   }
 
+  if ((st = streamer.finish(err))) return st;
   NvtxRange out_range("gnuts.nuts.copy_out");
   std::vector<Scal> sc(C);
   GN_CUDA(cudaMemcpy(sc.data(), B.sc, sizeof(Scal) * C, cudaMemcpyDeviceToHost));

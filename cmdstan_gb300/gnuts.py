@@ -37,7 +37,7 @@ EXPORTS = [
     "gnuts_flow_log_prob_grad", "gnuts_flow_log_prob_grad_tc", "gnuts_flow_adam_step", "gnuts_flow_train", "gnuts_hmc_nuts_flow_diag_e_adapt",
     "gnuts_learned_args_default", "gnuts_hmc_nuts_learned_diag_e_adapt", "gnuts_train_args_default",
     "gnuts_summary_columns_gpu",
-    "gnuts_diagnose",
+    "gnuts_diagnose", "gnuts_set_interrupt", "gnuts_set_draw_sink",
 ]
 SUMMARY_FIELDS = ["mean", "mcse", "sd", "mad"]
 
@@ -167,6 +167,9 @@ TIMING_FIELDS = ["rounds", "grad_kernel_us", "advance_kernel_us", "device_ms", "
 
 
 PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int)
+INTERRUPT_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p)
+DRAWS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double))
+ERR_INTERRUPTED = 7
 
 _lib = None
 
@@ -210,6 +213,10 @@ def load():
     lib.gnuts_summary.argtypes = [dp, ip, ip, i64, i64, dp, ip, dp]
     lib.gnuts_summary_columns.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, ip, dp]
     lib.gnuts_summary_columns_gpu.argtypes = [dp, ip, ip, ip, i64, i64, ctypes.POINTER(ip), dp, ip, dp]
+    lib.gnuts_set_interrupt.argtypes = [INTERRUPT_FN, ctypes.c_void_p]
+    lib.gnuts_set_interrupt.restype = None
+    lib.gnuts_set_draw_sink.argtypes = [DRAWS_FN, ctypes.c_void_p]
+    lib.gnuts_set_draw_sink.restype = None
     lib.gnuts_diagnose.argtypes = [dp, ip, ip, i64, i64, ip, ip, ip, ctypes.POINTER(ip), ip, ctypes.c_char_p, ip, ip,
                                    ip, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p]
     lib.gnuts_flow_create.argtypes = [ip, ip, ip, ctypes.c_double, ctypes.POINTER(vp)]
@@ -371,8 +378,13 @@ class Model:
         return Fit(SAMPLER_COLUMNS + self.param_names, b["draws"], b["eps"], minv, b["tw"], b["ts"], b["ng"],
                    b["stt"], b["nlf"], b["tim"][:len(TIMING_FIELDS)])
 
-    def sample(self, metric="diag_e", adapt=True, inits=None, inv_metric=None, progress=None, **kw):
-        """Run hmc_nuts_<metric>[_adapt]; keyword arguments are gnuts_sample_args fields."""
+    def sample(self, metric="diag_e", adapt=True, inits=None, inv_metric=None, progress=None, draw_sink=None,
+               interrupt=None, keep_draws=True, **kw):
+        """Run hmc_nuts_<metric>[_adapt]; keyword arguments are gnuts_sample_args fields.
+        draw_sink(first_row, rows) receives draw rows [chains, n, columns] while
+        the run proceeds (gnuts_set_draw_sink); interrupt() returning True stops
+        the run (gnuts_set_interrupt); keep_draws=False leaves the Fit's draws
+        empty (the sink has them)."""
         a = default_args(**kw)
         C, D = a.num_chains, self.dim
         mk = METRICS[metric]
@@ -391,10 +403,23 @@ class Model:
         cb = PROGRESS_FN(progress) if progress else PROGRESS_FN()
         name = "gnuts_hmc_nuts_%s%s" % (metric, "_adapt" if adapt else "")
         fn = getattr(self._lib, name)
-        if mk == 2:
-            rc = fn(self._h, ctypes.byref(a), _dp(inits), ctypes.byref(out), cb, None)
-        else:
-            rc = fn(self._h, ctypes.byref(a), _dp(inits), _dp(im), ctypes.byref(out), cb, None)
+        ncol = 7 + self.num_constrained
+        sink_cb = DRAWS_FN(lambda ctx, first, n, rows: draw_sink(
+            first, np.ctypeslib.as_array(rows, shape=(C, n, ncol)).copy())) if draw_sink else DRAWS_FN()
+        int_cb = INTERRUPT_FN(lambda ctx: 1 if interrupt() else 0) if interrupt else INTERRUPT_FN()
+        if not keep_draws:
+            out.draws = None
+            b["draws"] = np.zeros((C, 0, ncol))
+        self._lib.gnuts_set_draw_sink(sink_cb, None)
+        self._lib.gnuts_set_interrupt(int_cb, None)
+        try:
+            if mk == 2:
+                rc = fn(self._h, ctypes.byref(a), _dp(inits), ctypes.byref(out), cb, None)
+            else:
+                rc = fn(self._h, ctypes.byref(a), _dp(inits), _dp(im), ctypes.byref(out), cb, None)
+        finally:
+            self._lib.gnuts_set_draw_sink(DRAWS_FN(), None)
+            self._lib.gnuts_set_interrupt(INTERRUPT_FN(), None)
         _check(rc)
         return self._fit(b, mk)
 

@@ -29,6 +29,7 @@ extern "C" {
 #define GNUTS_ERR_SAMPLER 4     /* sampler error (improper posterior, metric overflow) */
 #define GNUTS_ERR_CUDA 5        /* CUDA runtime error / no device */
 #define GNUTS_ERR_TIMEOUT 6     /* a bounded device wait ran out */
+#define GNUTS_ERR_INTERRUPTED 7 /* the caller's interrupt callback asked the run to stop */
 
 /* gradient precision for data-heavy models */
 #define GNUTS_PRECISION_FP64 0   /* FP64 everywhere (CUDA cores) */
@@ -130,6 +131,29 @@ typedef struct {
 /* Progress callback, called from the calling thread between device launches
  * (mirrors the `Iteration: k / n [pct%]` logger lines). May be NULL. */
 typedef void (*gnuts_progress_fn)(void* ctx, int chain, int iteration, int total, int warmup);
+
+/* stan::callbacks::interrupt (created at command.hpp:186 and passed to every
+ * service at :609-688): a callback the service polls between device
+ * launches (every few milliseconds of sampling); a nonzero return stops the
+ * run, which then returns GNUTS_ERR_INTERRUPTED (rows already handed to a
+ * draw sink stay delivered; the gnuts_output arrays are not filled).
+ * Thread-local: it applies to the service calls of the calling thread made
+ * after it is set; NULL removes it. */
+typedef int (*gnuts_interrupt_fn)(void* ctx);
+void gnuts_set_interrupt(gnuts_interrupt_fn fn, void* ctx);
+
+/* Streaming draw output, the role of the sample_writers CmdStan hands the
+ * services (command.hpp:191-192, written per iteration): while a run of
+ * this thread proceeds, rows first_row .. first_row + n_rows - 1 of every
+ * chain are passed as soon as all chains have written them, as one
+ * [num_chains][n_rows][7 + num_constrained] block (same columns as
+ * gnuts_output.draws; the pointer is valid during the call).  With a sink
+ * set, gnuts_output.draws may be NULL, so the caller never holds all draws at
+ * once.  Blocks hold at most 64 MB; the last rows come when the run ends.
+ * Thread-local like gnuts_set_interrupt; NULL removes it.  Learned-map runs
+ * deliver their rows at the end of the run. */
+typedef void (*gnuts_draws_fn)(void* ctx, int first_row, int n_rows, const double* rows);
+void gnuts_set_draw_sink(gnuts_draws_fn fn, void* ctx);
 
 /* stan::services::sample::hmc_nuts_diag_e_adapt (command.hpp:673-688):
  * inits NULL -> random inits; inv_metric NULL -> unit diagonal start

@@ -435,8 +435,7 @@ int main(int argc, char** argv) {
     const std::string metric = hmc->child("metric")->value_text();
     Arg* out_grp = cfg.output.get();
     const std::string output_file = out_grp->child("file")->sval;
-    if (!out_grp->child("diagnostic_file")->sval.empty())
-      throw std::runtime_error("output diagnostic_file is not provided by gnuts-sample");
+    const std::string diagnostic_file = out_grp->child("diagnostic_file")->sval;
     const int sig_figs = (int)out_grp->child("sig_figs")->ival;
     const int prec = sig_figs < 0 ? 6 : sig_figs;
     const int refresh = (int)out_grp->child("refresh")->ival;
@@ -560,8 +559,15 @@ int main(int argc, char** argv) {
     std::vector<double> wsec(num_chains), ssec(num_chains), timing(GNUTS_TIMING_FIELDS);
     std::vector<int64_t> ngrad(num_chains), nlf(num_chains);
     std::vector<int> status(num_chains);
+    // diagnostic_file rows (command.hpp:225-247): sampler columns, q, p, g
+    std::vector<double> diag;
+    if (!diagnostic_file.empty()) {
+      if (learned) throw std::runtime_error("output diagnostic_file is not provided with gpu learned=1");
+      diag.resize((size_t)num_chains * n_saved * (7 + 3 * (size_t)D));
+    }
     gnuts_output out{};
     out.draws = draws.data();
+    out.diagnostics = diag.empty() ? nullptr : diag.data();
     out.stepsize = eps.data();
     out.inv_metric = minv.data();
     out.warmup_seconds = wsec.data();
@@ -683,6 +689,42 @@ int main(int argc, char** argv) {
     for (int c = 0; c < num_chains; ++c) {
       if (!chain_err[c].empty()) throw std::runtime_error(chain_err[c]);
       std::cout << chain_msg[c] << std::endl;
+    }
+
+    // ---- diagnostic_file per chain (file names as the output files', file.hpp:189-212):
+    // the config block, then one row per saved iteration
+    if (!diag.empty()) {
+      std::vector<std::string> unames;
+      for (int i = 0; i < D; ++i) {
+        gnuts_model_param_name(model, i, 1, nb, sizeof nb);
+        unames.push_back(nb);
+      }
+      const auto dnames = make_filenames(diagnostic_file, "", ".csv", num_chains, id);
+      const size_t dcol = 7 + 3 * (size_t)D;
+      for (int c = 0; c < num_chains; ++c) {
+        std::ofstream f(dnames[c]);
+        if (!f) throw std::runtime_error("Can't open diagnostic file " + dnames[c]);
+        f << "# stan_version_major = 2\n# stan_version_minor = 36\n# stan_version_patch = 0\n";
+        f << "# model = " << model_name << "\n# start_datetime = " << datetime << "\n";
+        for (auto& l : cfg_lines) f << "# " << l << "\n";
+        f << "lp__,accept_stat__,stepsize__,treedepth__,n_leapfrog__,divergent__,energy__";
+        for (auto& n : unames) f << "," << n;
+        for (auto& n : unames) f << ",p_" << n;
+        for (auto& n : unames) f << ",g_" << n;
+        f << "\n";
+        std::string line;
+        for (int r = 0; r < n_saved; ++r) {
+          const double* row = diag.data() + ((size_t)c * n_saved + r) * dcol;
+          line.clear();
+          for (size_t k = 0; k < dcol; ++k) {
+            if (k) line += ',';
+            line += fmt(row[k], prec);
+          }
+          line += '\n';
+          f << line;
+        }
+        if (!f) throw std::runtime_error("error writing " + dnames[c]);
+      }
     }
 
     // ---- adapted metric as JSON (command.hpp:247-261)

@@ -63,6 +63,8 @@ struct Params {
   int has_init, replay, n_saved, grad_budget;
   int cache;          // chain vectors cached in shared memory during a launch
   int cache_stride;   // doubles of shared memory per warp when cached
+  int diag;           // diagnostic rows wanted: track the selected point's momentum
+  int nrv;            // vectors per subtree record: 7, or 8 with diag (proposal momentum)
 };
 
 // vectors cached per chain (diag / unit metric also caches minv, wm, wm2)
@@ -77,7 +79,7 @@ constexpr int VCW = 8;
 struct Bufs {
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg;
   double *Tpb, *Tsb, *Tpe, *Tse, *Trho;
-  double* rec;   // [C][R][7][ld]
+  double* rec;   // [C][R][nrv][ld]
   double* recs;  // [C][R][3]: log-sum-weight, proposal lp, proposal energy of each record
   double* minv;  // diag/unit [C][ld]; dense [C][D][ld]
   double* chol;  // dense: transposed Cholesky factor Lt[k][i] = L[i][k], [C][D][ld]
@@ -89,12 +91,14 @@ struct Bufs {
   const double* p0;      // [C][D] (replay)
   const double* init_eps;  // [C] per-chain initial step size (null: P.stepsize)
   double* zdraws;        // [C][n_saved][D]: sampler-space draws (flow runs; write_array happens later)
+  double* Sp;            // [C][ld] momentum of the selected point (diag)
+  double* diag_draws;    // [C][n_saved][7 + 3D]: sampler columns, q, p, gradient (diag)
   Scal* sc;
   int* done_count;
 };
 
 // record vector slots
-enum { RV_PB = 0, RV_SB = 1, RV_PE = 2, RV_SE = 3, RV_RHO = 4, RV_Q = 5, RV_G = 6 };
+enum { RV_PB = 0, RV_SB = 1, RV_PE = 2, RV_SE = 3, RV_RHO = 4, RV_Q = 5, RV_G = 6, RV_P = 7 };
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -123,6 +127,7 @@ struct Chain {
   uint32_t chain_id;
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg, *Tpb, *Tsb, *Tpe, *Tse, *Trho;
   double *minv, *chol, *wm, *wm2, *tmp;
+  double* Sp;   // momentum of the selected point (diagnostic rows only)
   double* rsc;  // this chain's record scalars [R][3]
   double* cache_base = nullptr;
 
@@ -142,10 +147,11 @@ struct Chain {
     chol = p.metric == 1 ? b.chol + mo : nullptr;
     wm = b.wm + o;
     wm2 = b.wm2 + mo;
+    Sp = b.Sp ? b.Sp + o : nullptr;
   }
   __device__ __forceinline__ int metric() const { return MET >= 0 ? MET : P.metric; }
   __device__ double* rec(int r, int v) const {
-    return B.rec + (((size_t)c * P.R + r) * 7 + v) * P.ld;
+    return B.rec + (((size_t)c * P.R + r) * P.nrv + v) * P.ld;
   }
   // record scalars: every lane writes the same value; a full-warp shuffle or
   // __syncwarp separates reads from later writes of the same record
@@ -520,6 +526,8 @@ struct Chain {
         }
       }
     }
+    // the transition's sample starts as the starting point with its fresh momentum
+    if (P.diag) copy(Sp, Wp);
     s.F_lp = s.W_lp;
     s.B_lp = s.W_lp;
     s.lsw = 0;
@@ -602,6 +610,7 @@ struct Chain {
       }
     }
     if (take) copy2(Aq, Bq_, Ag, Bg_);
+    if (take && P.diag) copy(rec(A, RV_P), rec(Bk, RV_P));
     s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
     if (take) {
       const double lpB = rlp(Bk), hB = rh(Bk);
@@ -620,6 +629,7 @@ struct Chain {
     int r = alloc_rec();
     double *pb = rec(r, RV_PB), *sb = rec(r, RV_SB), *pe = rec(r, RV_PE), *se = rec(r, RV_SE),
            *rho = rec(r, RV_RHO), *rq = rec(r, RV_Q), *rg = rec(r, RV_G);
+    if (P.diag) copy(rec(r, RV_P), Wp);  // the leaf's proposal momentum (diagnostic rows)
     // p_sharp = minv p is formed in registers and stored to both ends of the
     // new leaf record (the dense metric needs the warp-wide product first)
     double kin = 0;
@@ -708,6 +718,7 @@ struct Chain {
            *Nrho = rec(N, RV_RHO), *Nq = rec(N, RV_Q), *Ng = rec(N, RV_G);
     if (take) {
       copy2(Sq, Nq, Sg, Ng);
+      if (P.diag) copy(Sp, rec(N, RV_P));
       s.S_lp = rlp(N);
       s.S_h = rh(N);
     }
@@ -765,6 +776,19 @@ struct Chain {
     if (lane == 0) {
       row[0] = s.S_lp; row[1] = accept; row[2] = s.eps; row[3] = s.depth;
       row[4] = s.n_leapfrog; row[5] = s.divergent; row[6] = s.S_h;
+    }
+    if (P.diag) {
+      // diagnostic_file row: sampler columns, unconstrained q, momentum p, gradient
+      double* dr = B.diag_draws + ((size_t)c * P.n_saved + s.row) * (7 + 3 * (size_t)P.D);
+      if (lane == 0) {
+        dr[0] = s.S_lp; dr[1] = accept; dr[2] = s.eps; dr[3] = s.depth;
+        dr[4] = s.n_leapfrog; dr[5] = s.divergent; dr[6] = s.S_h;
+      }
+      for (int d = lane; d < D; d += 32) {
+        dr[7 + d] = Sq[d];
+        dr[7 + P.D + d] = Sp[d];
+        dr[7 + 2 * P.D + d] = Sg[d];
+      }
     }
     if (B.zdraws) {
       double* zr = B.zdraws + ((size_t)c * P.n_saved + s.row) * P.D;

@@ -762,6 +762,9 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   P.replay = p0 != nullptr;
   P.n_saved = (a.save_warmup ? (a.num_warmup + a.thin - 1) / a.thin : 0) + (a.num_samples + a.thin - 1) / a.thin;
   P.grad_budget = 2048;
+  // diagnostic_file rows (plain runs; a flow run's sampler space is z)
+  P.diag = out && out->diagnostics && !rc.flow && !p0 ? 1 : 0;
+  P.nrv = P.diag ? 8 : 7;
   // cache the chain vectors in shared memory when four chains fit in a block's
   // budget.  It pays where a launch runs many steps of a chain (fused mode);
   // in round mode a launch runs one step and the copy in / out costs what it
@@ -792,7 +795,11 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   double** vecs[] = {&B.Wq, &B.Wp, &B.Wg, &B.Fq, &B.Fp, &B.Fg, &B.Bq, &B.Bp, &B.Bg, &B.Sq, &B.Sg,
                      &B.Tpb, &B.Tsb, &B.Tpe, &B.Tse, &B.Trho, &B.wm, &B.tmp};
   for (double** v : vecs) GN_CUDA(ar.alloc(v, vec));
-  GN_CUDA(ar.alloc(&B.rec, vec * P.R * 7));
+  GN_CUDA(ar.alloc(&B.rec, vec * P.R * P.nrv));
+  if (P.diag) {
+    GN_CUDA(ar.alloc(&B.Sp, vec));
+    GN_CUDA(ar.alloc(&B.diag_draws, (size_t)C * P.n_saved * (7 + 3 * (size_t)D)));
+  }
   GN_CUDA(ar.alloc(&B.recs, (size_t)C * P.R * 3));
   GN_CUDA(ar.alloc(&B.minv, mat));
   GN_CUDA(ar.alloc(&B.wm2, mat));
@@ -977,6 +984,9 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   if (out) {
     if (out->draws)
       GN_CUDA(cudaMemcpy(out->draws, B.draws, sizeof(double) * C * P.n_saved * P.ncol, cudaMemcpyDeviceToHost));
+    if (P.diag)
+      GN_CUDA(cudaMemcpy(out->diagnostics, B.diag_draws, sizeof(double) * C * P.n_saved * (7 + 3 * (size_t)D),
+                         cudaMemcpyDeviceToHost));
     if (out->stepsize) GN_CUDA(cudaMemcpy(out->stepsize, B.out_eps, sizeof(double) * C, cudaMemcpyDeviceToHost));
     if (out->inv_metric)
       GN_CUDA(cudaMemcpy(out->inv_metric, B.out_minv, sizeof(double) * C * msz, cudaMemcpyDeviceToHost));

@@ -133,7 +133,7 @@ class Output(ctypes.Structure):
     _fields_ = [("draws", ctypes.c_void_p), ("stepsize", ctypes.c_void_p), ("inv_metric", ctypes.c_void_p),
                 ("warmup_seconds", ctypes.c_void_p), ("sampling_seconds", ctypes.c_void_p),
                 ("n_grad", ctypes.c_void_p), ("chain_status", ctypes.c_void_p), ("n_leapfrog", ctypes.c_void_p),
-                ("timing", ctypes.c_void_p)]
+                ("timing", ctypes.c_void_p), ("diagnostics", ctypes.c_void_p)]
 
 
 class TrainArgs(ctypes.Structure):
@@ -379,12 +379,13 @@ class Model:
                    b["stt"], b["nlf"], b["tim"][:len(TIMING_FIELDS)])
 
     def sample(self, metric="diag_e", adapt=True, inits=None, inv_metric=None, progress=None, draw_sink=None,
-               interrupt=None, keep_draws=True, **kw):
+               interrupt=None, keep_draws=True, diagnostics=False, **kw):
         """Run hmc_nuts_<metric>[_adapt]; keyword arguments are gnuts_sample_args fields.
         draw_sink(first_row, rows) receives draw rows [chains, n, columns] while
         the run proceeds (gnuts_set_draw_sink); interrupt() returning True stops
         the run (gnuts_set_interrupt); keep_draws=False leaves the Fit's draws
-        empty (the sink has them)."""
+        empty (the sink has them); diagnostics=True also returns the
+        diagnostic_file rows as fit.diagnostics [chains, n, 7 + 3 D]."""
         a = default_args(**kw)
         C, D = a.num_chains, self.dim
         mk = METRICS[metric]
@@ -410,6 +411,9 @@ class Model:
         if not keep_draws:
             out.draws = None
             b["draws"] = np.zeros((C, 0, ncol))
+        diag = np.zeros((C, n_saved, 7 + 3 * D)) if diagnostics else None
+        if diag is not None:
+            out.diagnostics = diag.ctypes.data
         self._lib.gnuts_set_draw_sink(sink_cb, None)
         self._lib.gnuts_set_interrupt(int_cb, None)
         try:
@@ -421,7 +425,9 @@ class Model:
             self._lib.gnuts_set_draw_sink(DRAWS_FN(), None)
             self._lib.gnuts_set_interrupt(INTERRUPT_FN(), None)
         _check(rc)
-        return self._fit(b, mk)
+        fit = self._fit(b, mk)
+        fit.diagnostics = diag
+        return fit
 
     def sample_flow(self, flow, inits_z=None, inv_metric=None, **kw):
         """hmc_nuts_diag_e_adapt on z with x = flow(z); draws are reported in x."""

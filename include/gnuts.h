@@ -116,6 +116,10 @@ typedef struct {
   int* chain_status;         /* [num_chains] GNUTS_OK or the chain's error code */
   int64_t* n_leapfrog;       /* [num_chains] sum of n_leapfrog__ over all warmup + sampling iterations */
   double* timing;            /* [GNUTS_TIMING_FIELDS] run telemetry, see GNUTS_TIMING_* */
+  double* diagnostics;       /* [num_chains][n_saved][7 + 3 * num_params_r]: the rows of CmdStan's
+                                diagnostic_file (command.hpp:225-247): the seven sampler columns,
+                                then the selected point's unconstrained position q, its momentum p
+                                and the gradient g.  Plain (not learned-map) runs; NULL = not wanted */
 } gnuts_output;
 
 /* timing[] fields: device-side measurements of one run */

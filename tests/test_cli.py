@@ -374,3 +374,27 @@ def test_gpu_learned_run_writes_stan_csv(tmp_path):
                          "energy__"] and names[7] == "mu"
     assert len(rows) == 100
     assert any(l.startswith("#   learned = true") or l.startswith("# ") and "learned = true" in l for l in config)
+
+
+@pytest.mark.gpu
+def test_diagnostic_file_per_chain(tmp_path):
+    """diagnostic_file (command.hpp:225-247, multi_chain_test.cpp): one file per
+    chain named like the output files, columns lp__ .. energy__, the
+    unconstrained parameters, p_ and g_ of each; rows as the output file's."""
+    data = write_json(tmp_path / "bern.data.json", BERN_DATA)
+    rc, out, err = run(["model=bernoulli", "id=10", "sample", "num_samples=50", "num_warmup=100", "num_chains=2",
+                        "data", "file=" + data, "output", "file=b.csv", "diagnostic_file=b_diag.csv", "refresh=0"],
+                       tmp_path)
+    assert rc == 0, err
+    for k in (10, 11):
+        _, names, _, rows, _ = read_csv(tmp_path / ("b_%d.csv" % k))
+        lines = [l.strip() for l in open(tmp_path / ("b_diag_%d.csv" % k)) if not l.startswith("#")]
+        header = lines[0].split(",")
+        assert header[:7] == names[:7]
+        assert header[7:] == ["theta", "p_theta", "g_theta"]
+        drows = [[float(v) for v in l.split(",")] for l in lines[1:]]
+        assert len(drows) == len(rows) == 50
+        for d, r in zip(drows, rows):
+            assert d[:7] == r[:7]
+            # theta = inv_logit(q) (6 significant digits in both files)
+            assert abs(1 / (1 + pow(2.718281828459045, -d[7])) - r[7]) <= 1e-5

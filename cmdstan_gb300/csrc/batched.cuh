@@ -182,9 +182,80 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
   }
 }
 
+// reduce_gradient for the logistic model on the tensor-core path.  Every
+// load of the step -- the split partials, the lp partials, the linear part
+// and the chain's coefficients -- is issued before the arithmetic that needs
+// them (one memory round trip where the general path below takes seven:
+// its loops are ordered by stores the compiler must assume may alias).  The
+// results are bitwise those of the general path: the split partials are
+// summed in split order in FP32, the lp partials in split order in FP64 (one
+// shuffle per split), and each prior term takes its likelihood gradient from
+// the owning lane by shuffles instead of a store and reload.
+__device__ __forceinline__ double reduce_logistic_tc(const GradOut& G, const DevModel& M, int c, const double* q,
+                                                     double* g, int lane) {
+  const int K = M.K, S = G.S;
+  double qv[4];  // coefficient i = lane + 32 j (K + 1 <= 128)
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = lane + 32 * j;
+    qv[j] = i <= K ? q[i] : 0.0;
+  }
+  const double lin = G.lin[c];
+  const double lp0 = lane < S ? G.part_lp[(size_t)lane * G.C + c] : 0.0;  // splits 0..31, one per lane
+  const float4* src = reinterpret_cast<const float4*>(G.part_g32 + (size_t)c * TC_GSTRIDE) + lane;
+  const size_t stride = (size_t)G.C * TC_GSTRIDE / 4;
+  constexpr int SB = 16;  // splits loaded together
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int s0 = 0; s0 < S; s0 += SB) {
+    float4 v[SB];
+#pragma unroll
+    for (int u = 0; u < SB; ++u)
+      if (s0 + u < S) v[u] = src[(size_t)(s0 + u) * stride];
+#pragma unroll
+    for (int u = 0; u < SB; ++u)
+      if (s0 + u < S) {
+        a.x += v[u].x;
+        a.y += v[u].y;
+        a.z += v[u].z;
+        a.w += v[u].w;
+      }
+  }
+  double lp = 0;
+  for (int b = 0; b < S; b += 32) {
+    const double v = b == 0 ? lp0 : (b + lane < S ? G.part_lp[(size_t)(b + lane) * G.C + c] : 0.0);
+    const int n = min(32, S - b);
+    for (int u = 0; u < n; ++u) lp += __shfl_sync(GN_FULL, v, u);
+  }
+  lp += lin;
+  double pri = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    // coefficient i sits at position p = i - 1 (beta) or K (intercept), held by lane p / 4
+    const int i = lane + 32 * j;
+    const int pos = i == 0 ? K : i - 1;
+    const int own = (pos >> 2) & 31;
+    const float x0 = __shfl_sync(GN_FULL, a.x, own), x1 = __shfl_sync(GN_FULL, a.y, own);
+    const float x2 = __shfl_sync(GN_FULL, a.z, own), x3 = __shfl_sync(GN_FULL, a.w, own);
+    const int e = pos & 3;
+    const double t = (double)(e == 0 ? x0 : e == 1 ? x1 : e == 2 ? x2 : x3);
+    if (i <= K) {
+      const double v = qv[j];
+      if (i == 0) {
+        g[0] = t - v / 6.25;
+        pri += -0.5 * (v / 2.5) * (v / 2.5);
+      } else {
+        g[i] = t - v;
+        pri += -0.5 * v * v;
+      }
+    }
+  }
+  return lp + wsum(pri);
+}
+
 // sum the partials of chain c, add priors / Jacobian, write grad, return lp
 __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevModel& M, int c, const double* q,
                                                   double* g, int lane) {
+  if (G.part_g32 && G.lin && M.kind == MK_LOGISTIC && M.K + 1 <= 128) return reduce_logistic_tc(G, M, c, q, g, lane);
   const int K = M.K;
   // likelihood gradient wrt (b0, beta) -> g[0..K]; priors added below
   if (G.part_g32) sum_splits_f32(G, c, g, lane);

@@ -75,6 +75,7 @@ constexpr int NCACHE_VEC_DIAG = 20;
 // at most four vectors (leapfrog, leaf record, dot, metric product, copies)
 constexpr int VCH = 4;
 constexpr int VCW = 8;
+constexpr int VC1 = 4;  // elements per lane of the one-pass leaf step (D <= 128)
 
 struct Bufs {
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg;
@@ -254,6 +255,28 @@ struct Chain {
       }
     }
   }
+  __device__ void copy3(double* d1, const double* s1, double* d2, const double* s2, double* d3,
+                        const double* s3) const {
+    for (int base = 0; base < D; base += 32 * VCW) {
+      double u[VCW], v[VCW], w[VCW];
+#pragma unroll
+      for (int j = 0; j < VCW; ++j) {
+        const int d = base + lane + 32 * j;
+        u[j] = d < D ? s1[d] : 0.0;
+        v[j] = d < D ? s2[d] : 0.0;
+        w[j] = d < D ? s3[d] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < VCW; ++j) {
+        const int d = base + lane + 32 * j;
+        if (d < D) {
+          d1[d] = u[j];
+          d2[d] = v[j];
+          d3[d] = w[j];
+        }
+      }
+    }
+  }
   // The element loops below run in chunks of VCW elements per lane with every
   // load of a chunk issued before its arithmetic and stores: the vectors live
   // in global (or shared) memory behind pointers the compiler must assume may
@@ -385,9 +408,8 @@ struct Chain {
     return kinetic(Wp, ps) - s.W_lp;
   }
   __device__ void load_W_from(const double* q, const double* p, const double* g, double lp) {
-    copy(Wq, q);
-    if (p) copy(Wp, p);
-    copy(Wg, g);
+    if (p) copy3(Wq, q, Wp, p, Wg, g);
+    else copy2(Wq, q, Wg, g);
     s.W_lp = lp;
     __syncwarp();
   }
@@ -622,8 +644,97 @@ struct Chain {
     return (s1b > 0 && s1a > 0) && (s2b > 0 && s2a > 0) && (s3b > 0 && s3a > 0);
   }
 
+  // step_leaf for the diagonal and unit metrics when a chain's vectors fit one
+  // chunk of VC1 elements per lane (D <= 128): the leapfrog's second half step, the leaf record and
+  // -- when the doubling goes on without a merge -- the next leapfrog's first
+  // half step and position update run as one pass over registers, with one
+  // load of W (the separate steps take three memory round trips).  Same
+  // arithmetic, element by element and in each lane's order, as
+  // complete_leapfrog, the record loop of step_leaf and begin_leapfrog.
+  __device__ bool step_leaf_onepass(double e) {
+    ++s.n_grad;
+    ++s.n_leapfrog;
+    const int r = alloc_rec();
+    double *pb = rec(r, RV_PB), *sb = rec(r, RV_SB), *pe = rec(r, RV_PE), *se = rec(r, RV_SE),
+           *rho = rec(r, RV_RHO), *rq = rec(r, RV_Q), *rg = rec(r, RV_G);
+    double* rp = P.diag ? rec(r, RV_P) : nullptr;
+    double vp[VC1], vg[VC1], vq[VC1], vm[VC1];
+#pragma unroll
+    for (int j = 0; j < VC1; ++j) {
+      const int d = lane + 32 * j;
+      const bool ok = d < D;
+      vp[j] = ok ? Wp[d] : 0.0;
+      vg[j] = ok ? Wg[d] : 0.0;
+      vq[j] = ok ? Wq[d] : 0.0;
+      vm[j] = ok && metric() == 0 ? minv[d] : 0.0;
+    }
+    double kin = 0;
+#pragma unroll
+    for (int j = 0; j < VC1; ++j) {
+      const int d = lane + 32 * j;
+      if (d < D) {
+        const double p = vp[j] + 0.5 * e * vg[j];
+        vp[j] = p;
+        Wp[d] = p;
+        const double ps = metric() == 0 ? vm[j] * p : p;
+        kin += p * ps;
+        pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
+        rq[d] = vq[j]; rg[d] = vg[j];
+        if (rp) rp[d] = p;
+      }
+    }
+    double h = 0.5 * wsum(kin) - s.W_lp;
+    if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
+    if (h - s.H0 > 1000.0) s.divergent = 1;
+    s.sum_metro += (s.H0 - h > 0) ? 1.0 : exp(s.H0 - h);
+    rlsw(r) = s.H0 - h;
+    rlp(r) = s.W_lp;
+    rh(r) = h;
+    __syncwarp();
+    if (s.divergent) return end_transition();
+    if (!(s.leaf & 1) && s.depth != 0) {
+      // no pending subtree to merge and the doubling goes on: park the leaf at
+      // height 0 and start the next leapfrog from the registers
+      stack_set(0, r);
+      ++s.leaf;
+#pragma unroll
+      for (int j = 0; j < VC1; ++j) {
+        const int d = lane + 32 * j;
+        if (d < D) {
+          const double pn = vp[j] + 0.5 * e * vg[j];
+          Wp[d] = pn;
+          Wq[d] = vq[j] + e * (metric() == 0 ? vm[j] * pn : pn);
+        }
+      }
+      __syncwarp();
+      return true;
+    }
+    return after_leaf(r, e);
+  }
+
+  // merges of the new leaf r with the pending subtrees, then the end of the
+  // doubling or the next leapfrog
+  __device__ bool after_leaf(int r, double e) {
+    int cur = r, height = 0;
+    while ((s.leaf >> height) & 1) {
+      const int A = stack_get(height);
+      stack_set(height, 31);
+      bool ok = merge(A, cur);
+      free_rec(cur);
+      cur = A;
+      ++height;
+      if (!ok) return end_transition();
+    }
+    if (height == s.depth) return finish_doubling(cur);
+    stack_set(height, cur);
+    ++s.leaf;
+    begin_leapfrog(e);
+    return true;
+  }
+
   __device__ bool step_leaf() {
     const double e = s.dir * s.eps;
+    if (metric() != 1 && D <= 32 * VC1) return step_leaf_onepass(e);
     complete_leapfrog(e);
     ++s.n_leapfrog;
     int r = alloc_rec();
@@ -677,28 +788,14 @@ struct Chain {
     rh(r) = h;
     __syncwarp();
     if (s.divergent) return end_transition();
-    int cur = r, height = 0;
-    while ((s.leaf >> height) & 1) {
-      const int A = stack_get(height);
-      stack_set(height, 31);
-      bool ok = merge(A, cur);
-      free_rec(cur);
-      cur = A;
-      ++height;
-      if (!ok) return end_transition();
-    }
-    if (height == s.depth) return finish_doubling(cur);
-    stack_set(height, cur);
-    ++s.leaf;
-    begin_leapfrog(e);
-    return true;
+    return after_leaf(r, e);
   }
 
   __device__ bool finish_doubling(int N) {
     if (s.dir > 0) {
-      copy(Fq, Wq); copy(Fp, Wp); copy(Fg, Wg); s.F_lp = s.W_lp;
+      copy3(Fq, Wq, Fp, Wp, Fg, Wg); s.F_lp = s.W_lp;
     } else {
-      copy(Bq, Wq); copy(Bp, Wp); copy(Bg, Wg); s.B_lp = s.W_lp;
+      copy3(Bq, Wq, Bp, Wp, Bg, Wg); s.B_lp = s.W_lp;
     }
     ++s.depth;
     bool take;

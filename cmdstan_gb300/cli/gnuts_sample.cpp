@@ -591,7 +591,8 @@ int main(int argc, char** argv) {
         std::cout << "Learned preconditioner: " << (rep.used_flow ? "kept" : "rejected, plain NUTS kept")
                   << " (pilot ESS per gradient " << fmt(rep.flow_ess_per_grad, 3) << " vs "
                   << fmt(rep.plain_ess_per_grad, 3) << ", divergences " << fmt(rep.flow_divergence_rate, 3)
-                  << " vs " << fmt(rep.plain_divergence_rate, 3) << ")" << std::endl;
+                  << " vs " << fmt(rep.plain_divergence_rate, 3) << ", max R-hat " << fmt(rep.flow_max_rhat, 4)
+                  << " vs " << fmt(rep.plain_max_rhat, 4) << ")" << std::endl;
     } else if (engaged) {
       if (metric == "dense_e") rc = gnuts_hmc_nuts_dense_e_adapt(model, &a, ip, mp, &out, pf, &prog);
       else if (metric == "diag_e") rc = gnuts_hmc_nuts_diag_e_adapt(model, &a, ip, mp, &out, pf, &prog);

@@ -32,7 +32,7 @@ double now_s() {
 
 // per-sampler judge statistics over the constrained columns of pilot draws
 struct PilotStats {
-  double min_ess = 0, grads = 0, div_rate = 0;
+  double min_ess = 0, grads = 0, div_rate = 0, max_rhat = 0;
   std::vector<double> mean, mcse;
 };
 
@@ -50,6 +50,7 @@ PilotStats pilot_stats(const std::vector<double>& draws, int C, int n, int ncol)
     ps.mcse.push_back(o[1]);
     const double ess = std::isfinite(o[4]) ? o[4] : 0.0;
     ps.min_ess = std::min(ps.min_ess, ess);
+    ps.max_rhat = std::max(ps.max_rhat, std::isfinite(o[6]) ? o[6] : INFINITY);
   }
   double div = 0;
   for (int c = 0; c < C; ++c)
@@ -243,6 +244,7 @@ void gnuts_learned_args_default(gnuts_learned_args* la) {
   la->flow_delta = 0.95;
   la->pilot_samples = 200;
   la->moment_tolerance = 4.0;
+  la->rhat_max = 1.01;
 }
 
 int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args* a, const gnuts_learned_args* la,
@@ -355,10 +357,12 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
   const PilotStats sp = pilot_stats(rp.draws, C, P, ncol);
   rep.plain_ess_per_grad = sp.min_ess / std::max(1.0, sp.grads);
   rep.plain_divergence_rate = sp.div_rate;
+  rep.plain_max_rhat = sp.max_rhat;
   if (flow_ok) {
     const PilotStats sf = pilot_stats(rf.draws, C, P, ncol);
     rep.flow_ess_per_grad = sf.min_ess / std::max(1.0, sf.grads);
     rep.flow_divergence_rate = sf.div_rate;
+    rep.flow_max_rhat = sf.max_rhat;
     double zmax = 0;
     for (size_t k = 0; k < sp.mean.size(); ++k) {
       const double den = std::sqrt(sp.mcse[k] * sp.mcse[k] + sf.mcse[k] * sf.mcse[k]);
@@ -367,12 +371,16 @@ int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* mh, const gnuts_sample_args
     }
     rep.max_moment_z = zmax;
     const bool plain_clean = sp.div_rate <= 1e-3;
-    flow_ok = rep.flow_ess_per_grad >= rep.plain_ess_per_grad && sf.div_rate <= sp.div_rate &&
+    // the flow may not mix worse than the plain sampler, nor miss the
+    // convergence bound that the plain pilot meets
+    const bool rhat_ok = sf.max_rhat <= std::max(la->rhat_max, sp.max_rhat);
+    flow_ok = rep.flow_ess_per_grad >= rep.plain_ess_per_grad && sf.div_rate <= sp.div_rate && rhat_ok &&
               (!plain_clean || zmax <= la->moment_tolerance);
   } else {
     rep.flow_ess_per_grad = 0;
     rep.flow_divergence_rate = 1;
     rep.max_moment_z = INFINITY;
+    rep.flow_max_rhat = INFINITY;
   }
   rep.used_flow = flow_ok ? 1 : 0;
 

@@ -146,7 +146,7 @@ class LearnedArgs(ctypes.Structure):
     _fields_ = [("layers", ctypes.c_int), ("hidden", ctypes.c_int), ("clamp", ctypes.c_double),
                 ("train", TrainArgs), ("flow_warmup", ctypes.c_int), ("flow_delta", ctypes.c_double),
                 ("pilot_samples", ctypes.c_int),
-                ("moment_tolerance", ctypes.c_double)]
+                ("moment_tolerance", ctypes.c_double), ("rhat_max", ctypes.c_double)]
 
 
 class LearnedReport(ctypes.Structure):
@@ -156,7 +156,8 @@ class LearnedReport(ctypes.Structure):
                 ("loss_first", ctypes.c_double), ("loss_last", ctypes.c_double),
                 ("plain_seconds", ctypes.c_double), ("train_seconds", ctypes.c_double),
                 ("flow_seconds", ctypes.c_double), ("final_seconds", ctypes.c_double),
-                ("plain_grads", ctypes.c_int64), ("flow_grads", ctypes.c_int64), ("final_grads", ctypes.c_int64)]
+                ("plain_grads", ctypes.c_int64), ("flow_grads", ctypes.c_int64), ("final_grads", ctypes.c_int64),
+                ("plain_max_rhat", ctypes.c_double), ("flow_max_rhat", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -342,6 +342,7 @@ typedef struct {
   double flow_delta;        /* adaptation target of the z-space sampler, default 0.95 */
   int pilot_samples;        /* draws per chain each sampler produces for the judge, default 200 */
   double moment_tolerance;  /* combined MCSE, default 4 */
+  double rhat_max;          /* convergence bound on the pilots' max split R-hat, default 1.01 */
 } gnuts_learned_args;
 void gnuts_learned_args_default(gnuts_learned_args* la);
 
@@ -353,6 +354,7 @@ typedef struct {
   double loss_first, loss_last;     /* mean training loss of the first / last 10 steps */
   double plain_seconds, train_seconds, flow_seconds, final_seconds;
   int64_t plain_grads, flow_grads, final_grads;
+  double plain_max_rhat, flow_max_rhat;  /* max over parameters of the pilots' split R-hat */
 } gnuts_learned_report;
 
 /* Learned-preconditioner variant of hmc_nuts_diag_e_adapt (command.hpp:
@@ -362,8 +364,9 @@ typedef struct {
  * reverse KL through the model's own gradient kernels; (3) NUTS on z with
  * flow_warmup adaptive iterations and pilot_samples draws; (4) the judge
  * keeps the flow only if its ESS per gradient is not lower, its divergence
- * rate not higher and (when the plain pilot is free of divergences) every
- * posterior mean agrees within moment_tolerance combined MCSE; (5) the kept
+ * rate not higher, its max R-hat not above max(rhat_max, the plain pilot's)
+ * and (when the plain pilot is free of divergences) every posterior mean
+ * agrees within moment_tolerance combined MCSE; (5) the kept
  * sampler continues, non-adapting, for num_samples draws into out. */
 int gnuts_hmc_nuts_learned_diag_e_adapt(gnuts_model* m, const gnuts_sample_args* a, const gnuts_learned_args* la,
                                         const double* inits, gnuts_output* out, gnuts_learned_report* report,

@@ -171,10 +171,11 @@ def test_flow_sampler_is_exact_on_gaussian():
     assert np.allclose(fit.draws[:, :, 0], -0.5 * ((xs / scales) ** 2).sum(axis=2), rtol=1e-9, atol=1e-9)
 
 
-def _judge_expects(rep, tol=4.0):
+def _judge_expects(rep, tol=4.0, rhat_max=1.01):
     clean = rep["plain_divergence_rate"] <= 1e-3
     return int(rep["flow_ess_per_grad"] >= rep["plain_ess_per_grad"]
                and rep["flow_divergence_rate"] <= rep["plain_divergence_rate"]
+               and rep["flow_max_rhat"] <= max(rhat_max, rep["plain_max_rhat"])
                and (not clean or rep["max_moment_z"] <= tol))
 
 

@@ -36,14 +36,15 @@
 // X rows carry 104 BF16 columns (K predictors, the ones column, zeros), so
 // GEMM1 runs 7 K-steps of 16 (112 columns) and GEMM2 has N = 112.
 //
-// CTA = one 128-chain tile x one row split, 576 threads:
+// CTA = one 128-chain tile x one row split, 608 threads:
 //   warp 0       TMA producer: X row tiles (6-stage ring, 128 rows x 128
 //                predictors, SWIZZLE_128B)
-//   warp 1       MMA issuer (one thread) + TMEM owner
+//   warp 1       GEMM1 issuer (one thread) + TMEM owner
 //   warps 2..17  epilogue: thread = (chain, 32-row slice of the tile), four
 //                warps per TMEM lane quadrant; reads its H slice from TMEM and
 //                writes its 32 BF16 residuals back over the first 16 columns
 //                of that slice; y - 1/2 of the split is staged as floats
+//   warp 18      GEMM2 issuer (one thread)
 // TMEM (512 columns): two H buffers (128 each; each also carries the
 // residuals of its tile, GEMM2's A operand: lane = chain, two BF16 rows per
 // column), G (112, at 256), and the coefficient tile as GEMM1's A operand
@@ -52,13 +53,15 @@
 // memory holds only the X ring: an X tile is held from its load until GEMM2
 // of that tile retires (across GEMM1, the epilogue and GEMM2), and six stages
 // keep the next loads in flight behind the L2 latency (with two, the loads
-// sat on the critical path).  The MMA thread issues GEMM2 of tile t before
-// GEMM1 of tile t + 2, which overwrites the same buffer; tcgen05.mma
-// operations of one thread execute in issue order, so no barrier is needed
-// between the residual reads and that overwrite, nor between the epilogue's
-// reads of H and its residual writes (the slice's own columns, after
-// tcgen05.wait::ld).  GEMM1 of tile t+1 and GEMM2 of tile t-1 run while the
-// epilogue works on tile t.
+// sat on the critical path).  The two GEMMs are issued by two threads on
+// different warp schedulers: the epilogue's FP32 work takes most issue slots,
+// and one thread issuing both GEMMs plus their waits and commits left the
+// tensor pipe idle between tiles (6% slower).  GEMM1 of tile t + 2 overwrites
+// the buffer GEMM2 of tile t reads, so the GEMM1 thread waits on a commit
+// barrier of that GEMM2 (MMAs of different threads are not ordered).  No
+// barrier is needed between the epilogue's reads of H and its residual
+// writes (the slice's own columns, after tcgen05.wait::ld).  GEMM1 of tile
+// t+1 and GEMM2 of tile t-1 run while the epilogue works on tile t.
 // Every mbarrier wait is bounded; on expiry the kernel records an error,
 // drains what it issued and frees TMEM.
 #include <cuda.h>
@@ -67,15 +70,19 @@
 #include <cstring>
 #include <string>
 #include "grad_tc.h"
+#include "tc_ptx.cuh"
 
 namespace gnuts {
 namespace {
+
+using namespace tcx;
 
 constexpr int TILE_BYTES = 128 * 128 * 2;   // [2 k-halves][128 rows][64] BF16
 constexpr int HALF_BYTES = TILE_BYTES / 2;  // one k-half: 128 rows x 128 B
 constexpr int NS = 6;
 constexpr int EPI_WARPS = 16;                 // 4 per TMEM lane quadrant, 32 rows each
-constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
+constexpr int G2_WARP = 2 + EPI_WARPS;  // GEMM2 issuer
+constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS + 32;
 constexpr int MAX_SPLIT_ROWS = 6144;          // y of a whole row split staged as floats
 constexpr int OFF_X = 0;
 constexpr int OFF_BAR = OFF_X + NS * TILE_BYTES;  // 24 barriers
@@ -85,7 +92,6 @@ constexpr int OFF_Y = OFF_LP + 4 * 128 * 8;    // [MAX_SPLIT_ROWS] floats
 constexpr int SMEM_USED = OFF_Y + MAX_SPLIT_ROWS * 4;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;   // alignment slack
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t SPIN_LIMIT = 1u << 22;
 // K-steps of 16 columns that cover an X row of XTC_LD columns, and GEMM2's N
 constexpr int KSTEPS = (XTC_LD + 15) / 16;
 constexpr uint32_t GN = 16u * KSTEPS;
@@ -98,162 +104,9 @@ static_assert(TM_ALO + ACOLS <= TMEM_COLS && TM_G + 128 <= TM_AHI, "TMEM column 
 static_assert(ACOLS / 2 == 28, "each half-plane is written as x16 + x8 + x4 columns");
 
 // barrier indices
-enum { B_XFULL = 0, B_XEMPTY = NS, B_HFULL = 2 * NS, B_HFULL1, B_RFULL, B_RFULL1, B_GDONE, B_DRAIN, B_AREADY };
-static_assert(B_AREADY < 24, "barrier area holds 24 barriers");
-
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-// bounded wait for the phase with the given parity; false on timeout / abort
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
-  for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if ((i & 255u) == 255u && *abort) return false;
-  }
-  *abort = 1;
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// shared-memory matrix descriptor: SWIZZLE_128B, descriptor version 1
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-// instruction descriptor, kind::f16: D FP32, A/B BF16, M = 128, N = n (a multiple of 16)
-__host__ __device__ constexpr uint32_t idesc(bool a_mn, bool b_mn, uint32_t n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
-         ((n >> 3) << 17) | ((128u >> 4) << 24);
-}
-
-// A from tensor memory (lane = row of A, two BF16 per 32-bit column); the B
-// descriptor is passed as its two 32-bit halves: the issuing thread forms the
-// low half with one add per MMA (the address field is its low 14 bits and a
-// stage's addresses never carry out of it), the high half is fixed.
-__device__ __forceinline__ void mma_ta(uint32_t d, uint32_t a_tmem, uint32_t b_lo, uint32_t b_hi, uint32_t id,
-                                       uint32_t accum) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t.reg .b64 bd;\n\tsetp.ne.b32 p, %5, 0;\n\tmov.b64 bd, {%2, %3};\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], bd, %4, p;\n\t}" ::"r"(d),
-      "r"(a_tmem), "r"(b_lo), "r"(b_hi), "r"(id), "r"(accum)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-          taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-      : "memory");
-}
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* r) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
-               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
-               : "memory");
-}
-__device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t* r) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(r[0]), "r"(r[1]),
-               "r"(r[2]), "r"(r[3])
-               : "memory");
-}
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-// single-instruction approximations (SFU): 2^x, log2(x), 1/x
-__device__ __forceinline__ float ex2a(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float lg2a(float x) {
-  float y;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float rcpa(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-// Two FP32 lanes in one 64-bit register (element 0 in the low half) and the
-// packed f32x2 arithmetic of sm_100-class parts: one instruction per pair.
-// The epilogue does its FP32 work on pairs because scalar FP32 arithmetic at
-// full issue rate starves the single MMA-issuing thread of issue slots (it
-// shares a scheduler with four epilogue warps); the packed forms perform the
-// same IEEE operations in half the instructions.
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 f2pack(float a, float b) {
-  f2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ void f2unpack(f2 v, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
-__device__ __forceinline__ f2 f2add(f2 a, f2 b) {
-  f2 r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2 f2mul(f2 a, f2 b) {
-  f2 r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c) {
-  f2 r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<uint32_t*>(&v);
-}
+enum { B_XFULL = 0, B_XEMPTY = NS, B_HFULL = 2 * NS, B_HFULL1, B_RFULL, B_RFULL1, B_GDONE, B_DRAIN, B_AREADY,
+       B_G2DONE, B_G2DONE1, B_DRAIN2 };
+static_assert(B_DRAIN2 < 24, "barrier area holds 24 barriers");
 
 struct TcArgs {
   int N, K, C, Cpad, rows_per_split, S, C_total;
@@ -295,6 +148,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     mbar_init(bar(B_GDONE), 1);
     mbar_init(bar(B_DRAIN), 1);
     mbar_init(bar(B_AREADY), EPI_WARPS);
+    mbar_init(bar(B_G2DONE), 1);
+    mbar_init(bar(B_G2DONE1), 1);
+    mbar_init(bar(B_DRAIN2), 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -308,7 +164,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = *tmem_slot;
-  if (warp >= 2) {
+  if (warp >= 2 && warp < G2_WARP) {
     // GEMM1's A operand into TMEM: warp (quadrant q, sub) writes lanes 32q..32q+31
     // (chains c0 + 32q + lane), plane sub >> 1 (hi, lo), columns of half sub & 1
     const int q = warp & 3, sub = (warp - 2) >> 2;
@@ -331,7 +187,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     tmem_wait_st();
     fence_before();
     __syncwarp();
-    if (lane == 0) mbar_arrive(bar(B_AREADY));  // the MMA thread waits for all 16 before GEMM1
+    if (lane == 0) mbar_arrive(bar(B_AREADY));  // the GEMM1 thread waits for all 16
   }
 
   if (warp == 0) {
@@ -356,35 +212,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer
+    // ---------------- GEMM1 issuer: H(t) = coef . X(t)
     if (lane == 0) {
       const uint32_t ID1 = idesc(false, false, 128);  // A coef (TMEM), B = X K-major (N = 128 rows)
-      const uint32_t ID2 = idesc(false, true, GN);    // A = R (TMEM), B = X MN-major (N = GN predictors)
-      const uint32_t tG = tmem + TM_G;
       bool ok = mbar_wait(bar(B_AREADY), 0, abort);
-      // B descriptors of X stage 0: K-major for GEMM1, MN-major for GEMM2
-      const uint64_t d1 = sdesc(sbase + OFF_X, 0, 1024), d2 = sdesc(sbase + OFF_X, HALF_BYTES, 1024);
+      const uint64_t d1 = sdesc(sbase + OFF_X, 0, 1024);  // X stage 0, K-major
       const uint32_t d1lo = (uint32_t)d1, d1hi = (uint32_t)(d1 >> 32);
-      const uint32_t d2lo = (uint32_t)d2, d2hi = (uint32_t)(d2 >> 32);
-      // GEMM2 of tile u: G += R(u) . X(u); rows 16i .. 16i + 15 of R sit in
-      // columns 8i .. 8i + 7 of slice i / 2 (slice j starts at column 32 j)
-      auto gemm2 = [&](int u) -> bool {
-        const int rb = u & 1;
-        if (!mbar_wait(bar(B_RFULL + rb), (u >> 1) & 1, abort)) return false;
-        fence_after();
-        const uint32_t xlo = d2lo + (uint32_t)(((u % NS) * TILE_BYTES) >> 4);
-        const uint32_t tR = tmem + rb * 128;
-        const uint32_t acc0 = u > 0 ? 1u : 0u;
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-          mma_ta(tG, tR + (i >> 1) * 32 + (i & 1) * 8, xlo + (uint32_t)((i * 2048) >> 4), d2hi, ID2, i > 0 ? 1u : acc0);
-        mma_commit(bar(B_XEMPTY + u % NS));
-        return true;
-      };
-      int t = 0;
-      for (; ok && t < T; ++t) {
+      for (int t = 0; ok && t < T; ++t) {
         const int s = t % NS, b = t & 1;
-        if (!mbar_wait(bar(B_XFULL + s), (t / NS) & 1, abort)) { ok = false; break; }
+        if (!mbar_wait(bar(B_XFULL + s), (t / NS) & 1, abort)) break;
+        // buffer b still holds the residuals of tile t - 2 until its GEMM2 retires
+        if (t >= 2 && !mbar_wait(bar(B_G2DONE + b), ((t >> 1) - 1) & 1, abort)) break;
         fence_after();
         const uint32_t xlo = d1lo + (uint32_t)((s * TILE_BYTES) >> 4);
         const uint32_t tH = tmem + b * 128;
@@ -398,14 +236,37 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           }
         }
         mma_commit(bar(B_HFULL + b));
-        if (t >= 1 && !gemm2(t - 1)) { ok = false; break; }
       }
-      if (ok && T > 0) ok = gemm2(T - 1);
-      mma_commit(bar(B_GDONE));
       // drain every MMA this thread issued before TMEM is released
       mma_commit(bar(B_DRAIN));
       volatile int never = 0;
       mbar_wait(bar(B_DRAIN), 0, &never);
+    }
+  } else if (warp == G2_WARP) {
+    // ---------------- GEMM2 issuer: G += R(u) . X(u); rows 16i .. 16i + 15 of
+    // R sit in columns 8i .. 8i + 7 of slice i / 2 (slice j starts at column 32 j)
+    if (lane == 0) {
+      const uint32_t ID2 = idesc(false, true, GN);  // A = R (TMEM), B = X MN-major (N = GN predictors)
+      const uint32_t tG = tmem + TM_G;
+      const uint64_t d2 = sdesc(sbase + OFF_X, HALF_BYTES, 1024);
+      const uint32_t d2lo = (uint32_t)d2, d2hi = (uint32_t)(d2 >> 32);
+      for (int u = 0; u < T; ++u) {
+        const int rb = u & 1;
+        if (!mbar_wait(bar(B_RFULL + rb), (u >> 1) & 1, abort)) break;
+        fence_after();
+        const uint32_t xlo = d2lo + (uint32_t)(((u % NS) * TILE_BYTES) >> 4);
+        const uint32_t tR = tmem + rb * 128;
+        const uint32_t acc0 = u > 0 ? 1u : 0u;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          mma_ta(tG, tR + (i >> 1) * 32 + (i & 1) * 8, xlo + (uint32_t)((i * 2048) >> 4), d2hi, ID2, i > 0 ? 1u : acc0);
+        mma_commit(bar(B_XEMPTY + u % NS));
+        mma_commit(bar(B_G2DONE + rb));
+      }
+      mma_commit(bar(B_GDONE));
+      mma_commit(bar(B_DRAIN2));
+      volatile int never = 0;
+      mbar_wait(bar(B_DRAIN2), 0, &never);
     }
   } else {
     // ---------------- epilogue: 16 warps, thread = (chain, 32-row slice of the tile)
@@ -559,43 +420,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   if (threadIdx.x == 0 && *abort) atomicExch(A.error, 1);
 }
 
-using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiled get_encode(std::string& err) {
-  static EncodeTiled fn = nullptr;
-  if (fn) return fn;
-  void* p = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  // the entry point as introduced (CUDA 12.0)
-  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
-  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
-    err = "cuTensorMapEncodeTiled unavailable";
-    return nullptr;
-  }
-  fn = (EncodeTiled)p;
-  return fn;
-}
-
-int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
-             std::string& err) {
-  EncodeTiled enc = get_encode(err);
-  if (!enc) return GNUTS_ERR_CUDA;
-  cuuint64_t dims[2] = {inner, outer};
-  cuuint64_t strides[1] = {row_bytes};
-  cuuint32_t box[2] = {64, 128};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    err = "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r);
-    return GNUTS_ERR_CUDA;
-  }
-  return GNUTS_OK;
-}
-
 }  // namespace
 
 struct TcPlan {
@@ -646,7 +470,7 @@ int tc_create(const DevModel& M, int C, const int* done_count, TcPlan** out, uin
   // consumer sums whole 16-byte vectors
   if ((e = cudaMalloc(&p->part_g, sizeof(float) * S * C * TC_GSTRIDE)) != cudaSuccess) return fail(e);
   cudaMemset(p->part_g, 0, sizeof(float) * S * C * TC_GSTRIDE);
-  int rc = make_map(&p->xmap, M.Xtc, XTC_LD, (uint64_t)M.N, XTC_LD * 2, err);
+  int rc = make_map_bf16(&p->xmap, M.Xtc, XTC_LD, (uint64_t)M.N, XTC_LD * 2, 128, err);
   if (rc) {
     tc_destroy(p);
     return rc;

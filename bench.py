@@ -337,8 +337,8 @@ def bench_bernoulli():
 
 def bench_horseshoe(peaks, chains=256):
     """Config 5: regularised-horseshoe logistic regression, X 200,000 x 1000
-    (BF16-exact), 256 chains, diag_e, mixed precision (the cuBLASLt wide-design
-    gradient).  A bounded sampling run (30 warmup + 10 draws) gives
+    (BF16-exact), 256 chains, diag_e, mixed precision (the two-kernel tcgen05
+    wide-design gradient).  A bounded sampling run (30 warmup + 10 draws) gives
     grad-evals/s and the per-round kernel times; the wide gradient's roofline
     uses 4 N K C algorithmic flops per round.  The CPU baseline is the oracle's
     FP64 gradient on every host core."""
@@ -375,8 +375,9 @@ def bench_horseshoe(peaks, chains=256):
                          "peak": peaks.get("bf16_tflops_sustained", 1709.0), "unit": "TFLOP/s",
                          "frac": flops / (g_us * 1e-6) / 1e12 / peaks.get("bf16_tflops_sustained", 1709.0),
                          "note": "4*N*K flops per chain-gradient x 256 chains per round over the round's whole "
-                                 "gradient pipeline (coefficient staging, two cuBLASLt GEMMs with the hi/lo "
-                                 "split doubling GEMM1, the epilogue kernel)"},
+                                 "gradient pipeline (coefficient staging, the tcgen05 eta kernel with the hi/lo "
+                                 "split doubling its MMAs and the likelihood epilogue fused, the tcgen05 X^T r "
+                                 "kernel, the partial sums)"},
             "cpu_baseline": {"value": threads / cw, "unit": "grad-evals/s", "cores": threads, "kind": "port",
                              "sample": "%d oracle FP64 gradients, one per host thread, %.2f s" % (threads, cw)}}
 

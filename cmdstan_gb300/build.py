@@ -102,7 +102,7 @@ def build(verbose=False, jobs=None):
                 print(out)
     so = os.path.join(LIB, "libgnuts.so")
     if _newer(so, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart", "-lcublasLt"])
+        _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
     cli_src = os.path.join(CLI, "gnuts_sample.cpp")
     exe = os.path.join(LIB, "gnuts-sample")
     cli_deps = [os.path.join(CLI, f) for f in os.listdir(CLI)] if os.path.isdir(CLI) else []

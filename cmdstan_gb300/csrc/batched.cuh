@@ -37,7 +37,7 @@ struct GradOut {
   const int* done_count;
   int C_total;
   void* tc;           // tensor-core plan (grad_tc.cu), null for the SIMT path
-  void* wide;         // cuBLASLt plan for wide designs (grad_wide.cu), or null
+  void* wide;         // tcgen05 plan for wide designs (grad_wide.cu), or null
   uint16_t* coef_bf;  // tensor-core operand: [2][Cpad][128] BF16 hi / lo planes
   int Cpad;
   double* lin;        // [C] tensor-core path: linear likelihood part (hi + lo) . xtc_ym

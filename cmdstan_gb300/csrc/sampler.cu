@@ -310,21 +310,25 @@ int upload(Model& m, std::string& err) {
     if ((rc = dev_alloc(sizeof(float) * xn, (void**)&d.Xf))) return rc;
     if ((rc = dev_alloc(sizeof(uint16_t) * xn, (void**)&d.Xb))) return rc;
     const bool tc = h.kind == MK_LOGISTIC && h.K + 1 <= XTC_LD;
+    // y packed 32 rows per word for the tensor-core likelihood epilogues
+    const bool yb = (h.kind == MK_LOGISTIC || h.kind == MK_HORSESHOE) && h.yi;
     if (tc) {
       if ((rc = dev_alloc(sizeof(uint16_t) * (size_t)h.N * XTC_LD, (void**)&d.Xtc))) return rc;
-      if ((rc = dev_alloc(sizeof(uint32_t) * (((size_t)h.N + 31) / 32 + 4), (void**)&d.ybits))) return rc;
       if ((rc = dev_alloc(sizeof(double) * XTC_LD, (void**)&d.xtc_ym))) return rc;
     }
+    if (yb && (rc = dev_alloc(sizeof(uint32_t) * (((size_t)h.N + 31) / 32 + 4), (void**)&d.ybits))) return rc;
     k_derive_x<<<std::min<size_t>(4096, (xn + 255) / 256), 256>>>(d.X, xn, const_cast<float*>(d.Xf),
                                                                   const_cast<uint16_t*>(d.Xb));
     if (tc) {
       const size_t rows = (size_t)h.N;
       k_derive_xtc<<<std::min<size_t>(4096, (rows + 255) / 256), 256>>>(d.Xb, rows, h.K,
                                                                         const_cast<uint16_t*>(d.Xtc));
-      const size_t words = (rows + 31) / 32 + 4;
+      k_xtc_ym<<<XTC_LD, 256>>>(d.Xtc, d.yi, h.N, const_cast<double*>(d.xtc_ym));
+    }
+    if (yb) {
+      const size_t rows = (size_t)h.N, words = (rows + 31) / 32 + 4;
       k_pack_y<<<std::min<size_t>(4096, (words + 255) / 256), 256>>>(d.yi, rows, words,
                                                                      const_cast<uint32_t*>(d.ybits));
-      k_xtc_ym<<<XTC_LD, 256>>>(d.Xtc, d.yi, h.N, const_cast<double*>(d.xtc_ym));
     }
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { err = std::string("deriving X copies: ") + cudaGetErrorString(e); return GNUTS_ERR_CUDA; }
@@ -428,8 +432,8 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
     return GNUTS_OK;
   }
   if (prec == GNUTS_PRECISION_MIXED && wide_supported(M)) {
-    // wider than the tcgen05 tile: cuBLASLt GEMMs around this project's epilogue
-    int st = wide_create(M, C, &gs.wide, &G.coef64, &G.part_lp, &G.part_g, err);
+    // wider than k_glm_tc's tile: the two-kernel tcgen05 path
+    int st = wide_create(M, C, done_count, &gs.wide, &G.coef64, &G.part_lp, &G.part_g, err);
     if (st) return st;
     G.wide = gs.wide;
     G.S = 1;
@@ -452,10 +456,10 @@ int setup_grad(GradSetup& gs, const DevModel& M, int C, int prec, const int* don
   return GNUTS_OK;
 }
 
-// the batched contraction (tcgen05, cuBLASLt wide-design or SIMT); its
+// the batched contraction (tcgen05 narrow or wide design, or SIMT); its
 // partials are summed by the consumer (reduce_gradient, inside the
-// state-machine kernel).  Returns the cuBLASLt path's enqueue status; the
-// kernel paths report through the stream's launch errors.
+// state-machine kernel).  Returns the launch status of the wide-design path;
+// the others report through the stream's launch errors.
 int launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
   if (G.tc) {
     tc_launch((const TcPlan*)G.tc, st);

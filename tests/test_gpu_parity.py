@@ -349,11 +349,11 @@ def test_tensor_core_gradient_close_to_fp64(N, D, n):
     ("logistic", workloads.logistic(seed=12, N=8192, D=136)),
 ], ids=["horseshoe_256", "logistic_136"])
 def test_wide_gradient_close_to_fp64(mid, data):
-    """Designs wider than the tcgen05 tile go through cuBLASLt BF16 GEMMs
-    (coefficients split hi/lo, residuals BF16, FP32 accumulation) around the
-    project's epilogue kernel.  Same tolerances as the tcgen05 path: lp
-    relative 1e-4, gradient 2e-3 of its largest component; the FP64 path of
-    the same points stays at 1e-10."""
+    """Designs wider than k_glm_tc's tile go through the two-kernel tcgen05
+    path (k_wide_eta: eta with the likelihood epilogue fused, residuals BF16;
+    k_wide_xtr: X^T r), coefficients split hi/lo, FP32 accumulation.  Same
+    tolerances as the narrow tcgen05 path: lp relative 1e-4, gradient 2e-3 of
+    its largest component; the FP64 path of the same points stays at 1e-10."""
     gm, om = _pair(mid, data)
     rng = np.random.default_rng(17)
     q = rng.normal(0, 0.3, (9, gm.dim))
@@ -366,8 +366,26 @@ def test_wide_gradient_close_to_fp64(mid, data):
         assert abs(lp64[i] - olp) <= 1e-10 * abs(olp)
 
 
+def test_wide_gradient_ragged_shapes():
+    """Row count off every tile size (3001 rows: 256-row blocks of the eta
+    kernel, 64-row chunks of the X^T r kernel), predictors off the 64-column
+    chunk (200), and 130 chains: a second chain tile holding two chains."""
+    data = workloads.logistic(seed=14, N=3001, D=200)
+    gm, om = _pair("logistic", data)
+    q = np.random.default_rng(19).normal(0, 0.2, (130, gm.dim))
+    lp, g = gm.log_prob_grad(q, precision=gn.PRECISION_MIXED)
+    assert np.all(np.isfinite(lp)) and np.all(np.isfinite(g))
+    for i in (0, 1, 63, 127, 128, 129):
+        olp, og = om.log_prob_grad(q[i])
+        assert abs(lp[i] - olp) <= 1e-4 * abs(olp), (i, lp[i], olp)
+        assert np.max(np.abs(g[i] - og)) <= 2e-3 * np.max(np.abs(og)), (i, np.max(np.abs(g[i] - og)))
+    # same points again: the kernels' sums run in a fixed order
+    lp2, g2 = gm.log_prob_grad(q, precision=gn.PRECISION_MIXED)
+    assert np.array_equal(lp, lp2) and np.array_equal(g, g2)
+
+
 def test_wide_sampler_moments_match_oracle():
-    """NUTS on the cuBLASLt wide-design gradient: moments agree with the
+    """NUTS on the tcgen05 wide-design gradient: moments agree with the
     FP64 oracle's chains within 4.5 combined MCSE."""
     data = workloads.logistic(seed=22, N=8192, D=136)
     gm, om = _pair("logistic", data)

@@ -28,14 +28,15 @@
 //               G^T += r . X, A = r (K-major), B = X (MN-major, four 64-column
 //               boxes per chunk); one FP32 accumulator per CTA, written as a
 //               row-range partial.
-//   k_wide_final  fixed-order FP64 sums of the partials into the [C][K+1]
+//   k_wide_final  fixed-order sums of the partials into the [C][K+1]
 //               gradient and [C] lp rows that reduce_gradient consumes.
 //
 // Precision matches the tcgen05 path of narrow designs: X BF16-exact,
 // coefficients split into two BF16 parts (16 significant bits), FP32
 // accumulation, residuals BF16 in X^T r and exact (FP32) in the intercept
-// sum, per-thread sums in FP32 with a compensation term, per-block and
-// per-chain sums in FP64, all in a fixed order (bitwise reproducible).
+// sum; lp per thread in FP32 with a compensation term, per CTA and per chain
+// in FP64; the row ranges' X^T r partials summed in FP32; every sum in a
+// fixed order (bitwise reproducible).
 // Every mbarrier wait is bounded; on expiry a kernel records an error, drains
 // what it issued and frees its tensor memory.
 #include <cuda.h>
@@ -403,26 +404,50 @@ __global__ void k_wide_stage(const double* coef64, int C, int Cpad, int K, uint1
   }
 }
 
-// partials -> lp [C] and gradient rows [C][K+1] (intercept first), FP64
-// sums over the row ranges in order
-__global__ void k_wide_final(WideArgs A, double* part_lp, double* part_g) {
+// partials -> lp [C] and gradient rows [C][K+1] (intercept first).  Blocks
+// [0, nb_g): thread per (chain, predictor), the FP32 partials of the row
+// ranges summed in FP32 in range order (they are FP32 tensor-memory
+// accumulators; eight loads in flight per step); blocks after: warp per
+// chain, the eta kernel's FP64 lp and residual sums, lane l taking CTAs l,
+// l + 32, ... and a fixed butterfly.
+constexpr int F_THREADS = 256;
+__global__ void __launch_bounds__(F_THREADS) k_wide_final(WideArgs A, int nb_g, double* part_lp, double* part_g) {
   if (A.done_count && *A.done_count >= A.C_total) return;
   const int K1 = A.K + 1;
-  const size_t n = (size_t)A.C * K1;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i / K1), k = (int)(i % K1);
-    double s = 0.0;
-    if (k == 0) {
-      double l = 0.0;
-      for (int p = 0; p < A.P; ++p) {
-        s += A.prs[(size_t)p * A.C + c];
-        l += A.plp[(size_t)p * A.C + c];
-      }
-      part_lp[c] = l;
-    } else {
-      for (int p = 0; p < A.S2; ++p) s += (double)A.gpart[((size_t)p * A.Cpad + c) * A.Kp + (k - 1)];
+  if ((int)blockIdx.x < nb_g) {
+    const size_t i = (size_t)blockIdx.x * F_THREADS + threadIdx.x;
+    const int c = (int)(i / A.K), k = (int)(i % A.K);
+    if (c >= A.C) return;
+    const float* src = A.gpart + (size_t)c * A.Kp + k;
+    const size_t stride = (size_t)A.Cpad * A.Kp;
+    float s = 0.f;
+    for (int p0 = 0; p0 < A.S2; p0 += 8) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = p0 + u < A.S2 ? src[(size_t)(p0 + u) * stride] : 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (p0 + u < A.S2) s += v[u];
     }
-    part_g[i] = s;
+    part_g[(size_t)c * K1 + 1 + k] = (double)s;
+    return;
+  }
+  const int c = ((int)blockIdx.x - nb_g) * (F_THREADS / 32) + (int)(threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= A.C) return;
+  double l = 0.0, r = 0.0;
+  for (int p = lane; p < A.P; p += 32) {
+    l += A.plp[(size_t)p * A.C + c];
+    r += A.prs[(size_t)p * A.C + c];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l += __shfl_xor_sync(0xffffffffu, l, o);
+    r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  if (lane == 0) {
+    part_lp[c] = l;
+    part_g[(size_t)c * K1] = r;
   }
 }
 
@@ -525,8 +550,9 @@ int wide_launch(const WidePlan* p, const GradOut& G, const DevModel& M, cudaStre
   k_wide_stage<<<std::min(4096, (A.C * A.K + 255) / 256), 256, 0, st>>>(G.coef64, A.C, A.Cpad, A.K, p->planes);
   k_wide_eta<<<p->grid_eta, E_THREADS, E_SMEM, st>>>(p->cmap, p->xmap_eta, A);
   k_wide_xtr<<<p->grid_xtr, G_THREADS, G_SMEM, st>>>(p->rmap, p->xmap_xtr, A);
-  const size_t n = (size_t)A.C * (A.K + 1);
-  k_wide_final<<<(int)std::min<size_t>(4096, (n + 255) / 256), 256, 0, st>>>(A, G.part_lp, G.part_g);
+  const int nb_g = (int)(((size_t)A.C * A.K + F_THREADS - 1) / F_THREADS);
+  const int nb_c = (A.C + F_THREADS / 32 - 1) / (F_THREADS / 32);
+  k_wide_final<<<nb_g + nb_c, F_THREADS, 0, st>>>(A, nb_g, G.part_lp, G.part_g);
   return cudaGetLastError() == cudaSuccess ? GNUTS_OK : GNUTS_ERR_CUDA;
 }
 

@@ -30,6 +30,9 @@ CU_SOURCES = ["sampler.cu", "fused.cu", "grad_tc.cu", "grad_wide.cu", "noalloc.c
 # compiled once per model kind (-DGNUTS_KIND=k, k = 0..N_KINDS-1)
 CU_KIND_SOURCES = ["fused_kind.cu", "flow_tc_kind.cu"]
 N_KINDS = 7
+# compiled once per (metric, team width) of the round-mode state machine
+ADVANCE_SOURCE = "advance_kind.cu"
+ADVANCE_VARIANTS = [(m, tw) for tw in (32, 128) for m in (0, 1, 2)]
 CPP_SOURCES = ["abi.cpp", "summary.cpp", "learned.cpp", "diagnose.cpp"]
 
 
@@ -86,6 +89,12 @@ def build(verbose=False, jobs=None):
             objs.append(o)
             if _newer(o, [s] + headers):
                 cmds.append([nvcc] + NVCC_FLAGS + ["-DGNUTS_KIND=%d" % k, "-c", s, "-o", o])
+    s = os.path.join(CSRC, ADVANCE_SOURCE)
+    for m, tw in ADVANCE_VARIANTS:
+        o = os.path.join(objdir, "%s.m%d.t%d.o" % (ADVANCE_SOURCE, m, tw))
+        objs.append(o)
+        if _newer(o, [s] + headers):
+            cmds.append([nvcc] + NVCC_FLAGS + ["-DGNUTS_MET=%d" % m, "-DGNUTS_TW=%d" % tw, "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(objdir, src + ".o")

@@ -45,16 +45,17 @@ struct GradOut {
 
 // Sum the S row-split partials of chain c in a fixed order (s = 0, 1, ...):
 // FP32 sums for the mixed path, whose partials are FP32 tensor-memory
-// accumulators, FP64 otherwise.  Lane l owns coefficients l, l+32, ...; the
+// accumulators, FP64 otherwise.  Thread l of the team owns coefficients l,
+// l + TW, ...; the
 // loads of 8 splits x SCH coefficients are issued together.  out[i] receives
 // the sum for coefficient i (i <= K).
 constexpr int SCH = 4;  // coefficients per lane per pass
-template <class Acc>
+template <class Acc, int TW = 32>
 __device__ __forceinline__ void sum_splits(const GradOut& G, int c, double* out, int lane) {
   const int K1 = G.K + 1;
   const size_t stride = (size_t)G.C * K1;
   const double* src = G.part_g + (size_t)c * K1;
-  for (int base = 0; base < K1; base += 32 * SCH) {
+  for (int base = 0; base < K1; base += TW * SCH) {
     Acc acc[SCH];
 #pragma unroll
     for (int j = 0; j < SCH; ++j) acc[j] = 0;
@@ -64,7 +65,7 @@ __device__ __forceinline__ void sum_splits(const GradOut& G, int c, double* out,
       for (int u = 0; u < 8; ++u)
 #pragma unroll
         for (int j = 0; j < SCH; ++j) {
-          const int i = base + lane + 32 * j;
+          const int i = base + lane + TW * j;
           v[u][j] = (s0 + u < G.S && i < K1) ? src[(size_t)(s0 + u) * stride + i] : 0.0;
         }
 #pragma unroll
@@ -75,7 +76,7 @@ __device__ __forceinline__ void sum_splits(const GradOut& G, int c, double* out,
     }
 #pragma unroll
     for (int j = 0; j < SCH; ++j) {
-      const int i = base + lane + 32 * j;
+      const int i = base + lane + TW * j;
       if (i < K1) out[i] = (double)acc[j];
     }
   }
@@ -132,6 +133,7 @@ inline bool batched_supported(const DevModel& M) {
 
 // ---------------------------------------------------------------- staging
 // coefficient row of chain c from its unconstrained position q
+template <int TW = 32>
 __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& M, int c, const double* q,
                                               int lane) {
   const int K = M.K;
@@ -147,7 +149,7 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
       __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(G.coef_bf) + (size_t)c * 128;
       __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(G.coef_bf) + ((size_t)G.Cpad + c) * 128;
       double lin = 0;
-      for (int i = lane; i < 128; i += 32) {
+      for (int i = lane; i < 128; i += TW) {
         double v = i < K ? q[1 + i] : (i == K ? q[0] : 0.0);
         __nv_bfloat16 h = __float2bfloat16_rn((float)v);
         __nv_bfloat16 l = __float2bfloat16_rn((float)(v - (double)__bfloat162float(h)));
@@ -155,11 +157,11 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
         lo[i] = l;
         if (i < XTC_LD) lin += ((double)__bfloat162float(h) + (double)__bfloat162float(l)) * M.xtc_ym[i];
       }
-      lin = wsum(lin);
+      lin = tsum<TW>(lin);
       if (lane == 0) G.lin[c] = lin;
       return;
     }
-    for (int i = lane; i <= K; i += 32) {
+    for (int i = lane; i <= K; i += TW) {
       double v = q[i];
       o64[i] = v;
       if (o32) o32[i] = (float)v;
@@ -171,7 +173,21 @@ __device__ __forceinline__ void stage_request(const GradOut& G, const DevModel& 
       o64[0] = q[0];
       if (o32) o32[0] = (float)q[0];
     }
-    for (int d = lane; d < K; d += 32) {
+    if (G.prec == GNUTS_PRECISION_MIXED) {
+      // the coefficients feed a BF16 hi + lo split (16 significant bits):
+      // FP32 per coefficient, in the overflow-safe form
+      // lambda_tilde = sqrt(c2 / (c2 e + tau^2)) with e = 1 / lambda^2
+      const float c2f = (float)c2, t2f = (float)(tau * tau), tf = (float)tau;
+      for (int d = lane; d < K; d += TW) {
+        const float e = expf(-2.0f * (float)q[K + 2 + d]);
+        const float lamt = sqrtf(c2f / fmaf(c2f, e, t2f));
+        const double b = (double)((float)q[1 + d] * lamt * tf);
+        o64[1 + d] = b;
+        if (o32) o32[1 + d] = (float)b;
+      }
+      return;
+    }
+    for (int d = lane; d < K; d += TW) {
       double lam = exp(q[K + 2 + d]);
       double l2 = lam * lam;
       double lamt = sqrt(c2 * l2 / (c2 + tau * tau * l2));
@@ -253,21 +269,28 @@ __device__ __forceinline__ double reduce_logistic_tc(const GradOut& G, const Dev
 }
 
 // sum the partials of chain c, add priors / Jacobian, write grad, return lp
+template <int TW = 32>
 __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevModel& M, int c, const double* q,
                                                   double* g, int lane) {
-  if (G.part_g32 && G.lin && M.kind == MK_LOGISTIC && M.K + 1 <= 128) return reduce_logistic_tc(G, M, c, q, g, lane);
+  if constexpr (TW == 32) {
+    if (G.part_g32 && G.lin && M.kind == MK_LOGISTIC && M.K + 1 <= 128) return reduce_logistic_tc(G, M, c, q, g, lane);
+  }
   const int K = M.K;
   // likelihood gradient wrt (b0, beta) -> g[0..K]; priors added below
-  if (G.part_g32) sum_splits_f32(G, c, g, lane);
-  else if (G.prec == GNUTS_PRECISION_FP64) sum_splits<double>(G, c, g, lane);
-  else sum_splits<float>(G, c, g, lane);
+  if (G.part_g32) {
+    if (TW == 32 || lane < 32) sum_splits_f32(G, c, g, lane);  // 32 lanes x 4 positions
+  } else if (G.prec == GNUTS_PRECISION_FP64) {
+    sum_splits<double, TW>(G, c, g, lane);
+  } else {
+    sum_splits<float, TW>(G, c, g, lane);
+  }
   double lp = sum_split_lp(G, c);
   if (G.lin) lp += G.lin[c];
-  __syncwarp();
+  tsync<TW>();
   const double* gs = g;
   if (M.kind == MK_LOGISTIC) {
     double pri = 0;
-    for (int i = lane; i <= K; i += 32) {
+    for (int i = lane; i <= K; i += TW) {
       const double t = gs[i];
       double v = q[i];
       if (i == 0) {
@@ -278,33 +301,67 @@ __device__ __forceinline__ double reduce_gradient(const GradOut& G, const DevMod
         pri += -0.5 * v * v;
       }
     }
-    return lp + wsum(pri);
+    return lp + tsum<TW>(pri);
   }
   // horseshoe
   const double nu = M.slab_df, ssl = M.slab_scale, sg = M.scale_global;
   double lt = q[K + 1], tau = exp(lt), lc = q[2 * K + 2], caux = exp(lc);
   double c2 = ssl * ssl * caux;
   double pri = 0, glt = 0, glc = 0;
-  for (int d = lane; d < K; d += 32) {
-    const double t = gs[1 + d];
-    double z = q[1 + d];
-    double ll = q[K + 2 + d];
-    double lam = exp(ll);
-    double l2 = lam * lam;
-    double den = c2 + tau * tau * l2;
-    double a = c2 / den, bt = tau * tau * l2 / den;
-    double lamt = sqrt(c2 * l2 / den);
-    double beta = z * lamt * tau;
-    double gbd = t * beta;
-    pri += -0.5 * z * z - log1p(l2) + ll;
-    g[1 + d] = t * lamt * tau - z;
-    g[K + 2 + d] = gbd * a - 2.0 * l2 / (1.0 + l2) + 1.0;
-    glt += gbd * (1.0 - bt);
-    glc += gbd * 0.5 * bt;
+  if (G.prec == GNUTS_PRECISION_MIXED) {
+    // The chain rule through the per-coefficient transform in FP32 (its
+    // input, the likelihood gradient, carries BF16 residual error), in forms
+    // that stay finite wherever the FP32 exponentials do: with
+    // e = 1 / lambda^2 and r = tau^2 lambda^2 / c2,
+    //   a = c2 / (c2 + tau^2 lambda^2) = 1 / (1 + r),  bt = 1 - a = r / (1 + r),
+    //   lambda_tilde = sqrt(c2 / (c2 e + tau^2)),  lambda^2 / (1 + lambda^2) = 1 / (1 + e),
+    //   log1p(lambda^2) = 2 log(lambda) + log1p(e) (log lambda > 0), log1p(1 / e) otherwise.
+    // The per-lane sums of the prior and of the tau / c chain-rule terms are FP64.
+    const float c2f = (float)c2, t2f = (float)(tau * tau), tf = (float)tau;
+    const float lrat = (float)(2.0 * lt - log(c2));
+    for (int d = lane; d < K; d += TW) {
+      const float t = (float)gs[1 + d];
+      const float z = (float)q[1 + d];
+      const float ll = (float)q[K + 2 + d];
+      const float e = expf(-2.0f * ll);
+      const float r = expf(fmaf(2.0f, ll, lrat));
+      const float a = 1.0f / (1.0f + r);
+      const float bt = r < 1.0f ? r * a : 1.0f - a;
+      const float lamt = sqrtf(c2f / fmaf(c2f, e, t2f));
+      const float gbd = t * (z * lamt * tf);
+      const float l1p = ll > 0.0f ? fmaf(2.0f, ll, log1pf(e)) : log1pf(1.0f / e);
+      pri += (double)(fmaf(-0.5f * z, z, ll) - l1p);
+      g[1 + d] = (double)fmaf(t * lamt, tf, -z);
+      g[K + 2 + d] = (double)(fmaf(gbd, a, 1.0f) - 2.0f / (1.0f + e));
+      glt += (double)(gbd * a);  // 1 - bt
+      glc += (double)(gbd * 0.5f * bt);
+    }
+  } else {
+    for (int d = lane; d < K; d += TW) {
+      const double t = gs[1 + d];
+      double z = q[1 + d];
+      double ll = q[K + 2 + d];
+      double lam = exp(ll);
+      double l2 = lam * lam;
+      double den = c2 + tau * tau * l2;
+      double a = c2 / den, bt = tau * tau * l2 / den;
+      double lamt = sqrt(c2 * l2 / den);
+      double beta = z * lamt * tau;
+      double gbd = t * beta;
+      pri += -0.5 * z * z - log1p(l2) + ll;
+      g[1 + d] = t * lamt * tau - z;
+      g[K + 2 + d] = gbd * a - 2.0 * l2 / (1.0 + l2) + 1.0;
+      glt += gbd * (1.0 - bt);
+      glc += gbd * 0.5 * bt;
+    }
   }
-  pri = wsum(pri);
-  glt = wsum(glt);
-  glc = wsum(glc);
+  {
+    double v3[3] = {pri, glt, glc};
+    tsum_n<TW, 3>(v3);
+    pri = v3[0];
+    glt = v3[1];
+    glc = v3[2];
+  }
   double b0 = q[0];
   double ts = tau / sg;
   lp += pri - 0.5 * (b0 / 2.5) * (b0 / 2.5) - log1p(ts * ts) + (-0.5 * nu - 1.0) * lc - 0.5 * nu / caux + lt + lc;

@@ -24,6 +24,50 @@ __device__ __forceinline__ double wsum(double v) {
 }
 __device__ __forceinline__ bool wall(bool p) { return __all_sync(GN_FULL, p); }
 
+// Team primitives.  A team of TW threads advances one chain: one warp
+// (TW = 32), or the whole CTA (TW a multiple of 32 up to 1024).  Every
+// thread of the team receives the same bits: the warp butterfly combines
+// symmetric pairs, and the per-warp values are added by every thread in warp
+// order.  TW = 32 is exactly the warp code.
+template <int TW>
+__device__ __forceinline__ void tsync() {
+  if constexpr (TW == 32) __syncwarp();
+  else __syncthreads();
+}
+template <int TW, int N>
+__device__ __forceinline__ void tsum_n(double (&v)[N]) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = wsum(v[i]);
+  if constexpr (TW > 32) {
+    constexpr int NW = TW / 32;
+    __shared__ double red[N * NW];
+    __syncthreads();  // earlier readers of red are done
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) red[i * NW + (threadIdx.x >> 5)] = v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      double t = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) t += red[i * NW + w];
+      v[i] = t;
+    }
+  }
+}
+template <int TW>
+__device__ __forceinline__ double tsum(double v) {
+  double a[1] = {v};
+  tsum_n<TW, 1>(a);
+  return a[0];
+}
+template <int TW>
+__device__ __forceinline__ bool tall(bool p) {
+  if constexpr (TW == 32) return wall(p);
+  else return __syncthreads_and(p) != 0;
+}
+
 __device__ __forceinline__ double log1p_exp(double a) {
   return a > 0 ? a + log1p(exp(-a)) : log1p(exp(a));
 }
@@ -396,7 +440,9 @@ __device__ __forceinline__ const DevModel& chain_model(const DevModel& M, int c,
   return M.members ? M.members[c / (C / M.n_members)] : M;
 }
 
-// write_array: unconstrained q -> constrained output columns (warp-parallel)
+// write_array: unconstrained q -> constrained output columns (team-parallel:
+// thread `lane` of TW)
+template <int TW = 32>
 __device__ __forceinline__ void warp_write_array(const DevModel& M, const double* q, double* out,
                                                  int lane) {
   switch (M.kind) {
@@ -406,22 +452,22 @@ __device__ __forceinline__ void warp_write_array(const DevModel& M, const double
     case MK_NORMAL:
     case MK_LOGISTIC:
     case MK_FUNNEL:
-      for (int i = lane; i < M.D; i += 32) out[i] = q[i];
+      for (int i = lane; i < M.D; i += TW) out[i] = q[i];
       return;
     case MK_HIER:
-      for (int i = lane; i < M.D; i += 32) out[i] = (i == M.J + 1) ? exp(q[i]) : q[i];
+      for (int i = lane; i < M.D; i += TW) out[i] = (i == M.J + 1) ? exp(q[i]) : q[i];
       return;
     case MK_VARINT: {
       const int is = M.alpha_last ? M.K : M.J + M.K;
-      for (int i = lane; i < M.D; i += 32) out[i] = (i == is || i == is + 1) ? exp(q[i]) : q[i];
+      for (int i = lane; i < M.D; i += TW) out[i] = (i == is || i == is + 1) ? exp(q[i]) : q[i];
       return;
     }
     case MK_HORSESHOE: {
       const int D = M.K;
       double tau = exp(q[D + 1]), caux = exp(q[2 * D + 2]);
       double c2 = M.slab_scale * M.slab_scale * caux;
-      for (int i = lane; i < 2 * D + 3; i += 32) out[i] = (i <= D) ? q[i] : exp(q[i]);
-      for (int d = lane; d < D; d += 32) {
+      for (int i = lane; i < 2 * D + 3; i += TW) out[i] = (i <= D) ? q[i] : exp(q[i]);
+      for (int d = lane; d < D; d += TW) {
         double lam = exp(q[D + 2 + d]);
         double l2 = lam * lam;
         double lamt = sqrt(c2 * l2 / (c2 + tau * tau * l2));

@@ -13,8 +13,11 @@
 // {p_beg, p#_beg, p_end, p#_end, rho, proposal q, proposal grad} addressed by
 // index, so merges and pushes move indices, not vectors.
 //
-// One warp advances one chain; lane l owns vector elements l, l+32, ...
-// Every lane carries the same scalar state (lane-uniform control flow).
+// A team of TW threads advances one chain -- one warp (TW = 32), or a CTA
+// (TW = 256) for wide chains, whose per-element work would otherwise run 63
+// elements deep per lane on one warp scheduler; thread l owns vector elements
+// l, l + TW, ...  Every thread carries the same scalar state (team-uniform
+// control flow); team sums hand every thread the same bits.
 // advance() runs the machine until the chain needs the gradient at W.q (it
 // returns true) or the chain is finished (false).  The gradient is written
 // into W.g / W_lp by the caller: inline (fused kernel) or by a batched
@@ -118,7 +121,7 @@ __device__ __forceinline__ double lse(double a, double b) {
 // MET >= 0 fixes the metric at compile time (0 diag_e, 1 dense_e, 2 unit_e):
 // a kernel instantiated per metric carries only that metric's code on its
 // hot path; MET = -1 reads it from the run's parameters.
-template <int MET = -1>
+template <int MET = -1, int TW = 32>
 struct Chain {
   const Params& P;
   const Bufs& B;
@@ -196,58 +199,58 @@ struct Chain {
     for_each_cached([&](int i, double** p) {
       const double* gsrc = *p;
       double* sm = base + (size_t)i * P.ld;
-      for (int d = lane; d < D; d += 32) cp_async8(sm + d, gsrc + d);
+      for (int d = lane; d < D; d += TW) cp_async8(sm + d, gsrc + d);
       *p = sm;
     });
     double* sr = base + (size_t)cached_vectors() * P.ld;
-    for (int i = lane; i < P.R * 3; i += 32) cp_async8(sr + i, rsc + i);
+    for (int i = lane; i < P.R * 3; i += TW) cp_async8(sr + i, rsc + i);
     rsc = sr;
     asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncwarp();
+    tsync<TW>();
   }
   __device__ void cache_detach() {
-    __syncwarp();
+    tsync<TW>();
     const size_t o = (size_t)c * P.ld;
     double* g[NCACHE_VEC_DIAG] = {B.Wq + o, B.Wp + o, B.Wg + o, B.Fq + o, B.Fp + o, B.Fg + o, B.Bq + o,
                                   B.Bp + o, B.Bg + o, B.Sq + o, B.Sg + o, B.Tpb + o, B.Tsb + o, B.Tpe + o,
                                   B.Tse + o, B.Trho + o, B.tmp + o, B.minv + o, B.wm + o, B.wm2 + o};
     for_each_cached([&](int i, double** p) {
-      for (int d = lane; d < D; d += 32) g[i][d] = (*p)[d];
+      for (int d = lane; d < D; d += TW) g[i][d] = (*p)[d];
     });
     double* gr = B.recs + (size_t)c * P.R * 3;
-    for (int i = lane; i < P.R * 3; i += 32) gr[i] = rsc[i];
+    for (int i = lane; i < P.R * 3; i += TW) gr[i] = rsc[i];
   }
 
   // ---------------- vector helpers ----------------
   // chunks of VCW elements per lane: every load of a chunk is issued before
-  // its stores, so a copy costs one memory round trip per 32 VCW elements
+  // its stores, so a copy costs one memory round trip per TW VCW elements
   __device__ void copy(double* dst, const double* src) const {
-    for (int base = 0; base < D; base += 32 * VCW) {
+    for (int base = 0; base < D; base += TW * VCW) {
       double v[VCW];
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         v[j] = d < D ? src[d] : 0.0;
       }
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (d < D) dst[d] = v[j];
       }
     }
   }
   __device__ void copy2(double* d1, const double* s1, double* d2, const double* s2) const {
-    for (int base = 0; base < D; base += 32 * VCW) {
+    for (int base = 0; base < D; base += TW * VCW) {
       double v[VCW], w[VCW];
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         v[j] = d < D ? s1[d] : 0.0;
         w[j] = d < D ? s2[d] : 0.0;
       }
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (d < D) {
           d1[d] = v[j];
           d2[d] = w[j];
@@ -257,18 +260,18 @@ struct Chain {
   }
   __device__ void copy3(double* d1, const double* s1, double* d2, const double* s2, double* d3,
                         const double* s3) const {
-    for (int base = 0; base < D; base += 32 * VCW) {
+    for (int base = 0; base < D; base += TW * VCW) {
       double u[VCW], v[VCW], w[VCW];
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         u[j] = d < D ? s1[d] : 0.0;
         v[j] = d < D ? s2[d] : 0.0;
         w[j] = d < D ? s3[d] : 0.0;
       }
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (d < D) {
           d1[d] = u[j];
           d2[d] = v[j];
@@ -285,40 +288,40 @@ struct Chain {
   // summation order are those of the plain loop.
   __device__ double dot(const double* a, const double* b) const {
     double t = 0;
-    for (int base = 0; base < D; base += 32 * VCW) {
+    for (int base = 0; base < D; base += TW * VCW) {
       double va[VCW], vb[VCW];
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         va[j] = d < D ? a[d] : 0.0;
         vb[j] = d < D ? b[d] : 0.0;
       }
 #pragma unroll
       for (int j = 0; j < VCW; ++j)
-        if (base + lane + 32 * j < D) t += va[j] * vb[j];
+        if (base + lane + TW * j < D) t += va[j] * vb[j];
     }
-    return wsum(t);
+    return tsum<TW>(t);
   }
   // out = minv * p  (p must be visible to the whole warp for dense)
   __device__ void dtau(double* out, const double* p) const {
     if (metric() != 1) {
-      for (int base = 0; base < D; base += 32 * VCW) {
+      for (int base = 0; base < D; base += TW * VCW) {
         double vm[VCW], vp[VCW];
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
-          const int d = base + lane + 32 * j;
+          const int d = base + lane + TW * j;
           vp[j] = d < D ? p[d] : 0.0;
           vm[j] = d < D && metric() == 0 ? minv[d] : 0.0;
         }
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
-          const int d = base + lane + 32 * j;
+          const int d = base + lane + TW * j;
           if (d < D) out[d] = metric() == 0 ? vm[j] * vp[j] : vp[j];
         }
       }
     } else {
-      __syncwarp();
-      for (int d = lane; d < D; d += 32) {
+      tsync<TW>();
+      for (int d = lane; d < D; d += TW) {
         double t = 0;
         for (int j = 0; j < D; ++j) t += minv[(size_t)j * P.ld + d] * p[j];
         out[d] = t;
@@ -331,41 +334,41 @@ struct Chain {
   __device__ void sample_p(double* p) {
     const uint64_t n0 = s.rng_n;
     if (metric() == 1) {
-      for (int d = lane; d < D; d += 32) tmp[d] = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
-      __syncwarp();
+      for (int d = lane; d < D; d += TW) tmp[d] = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
+      tsync<TW>();
       // solve Lt p = z, back substitution over rows of Lt (Lt[i][k] = L[k][i])
       for (int i = D - 1; i >= 0; --i) {
         const double* row = chol + (size_t)i * P.ld;
         double t = 0;
-        for (int k = i + 1 + lane; k < D; k += 32) t += row[k] * p[k];
-        t = wsum(t);
+        for (int k = i + 1 + lane; k < D; k += TW) t += row[k] * p[k];
+        t = tsum<TW>(t);
         double v = (tmp[i] - t) / row[i];
-        if (lane == (i & 31)) p[i] = v;
-        __syncwarp();
+        if (lane == i % TW) p[i] = v;
+        tsync<TW>();
       }
     } else {
-      for (int d = lane; d < D; d += 32) {
+      for (int d = lane; d < D; d += TW) {
         double z = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
         p[d] = metric() == 0 ? z / sqrt(minv[d]) : z;
       }
     }
     s.rng_n = n0 + (uint64_t)((D + 1) / 2);
-    __syncwarp();
+    tsync<TW>();
   }
   __device__ double uniform() { return rng_uniform(P.seed, chain_id, 0u, s.rng_n++); }
 
   // W.p += e/2 g ; W.q += e * minv W.p   (gradient at W.q then requested)
   __device__ void begin_leapfrog(double e) {
     if (metric() == 1) {
-      for (int d = lane; d < D; d += 32) Wp[d] += 0.5 * e * Wg[d];
+      for (int d = lane; d < D; d += TW) Wp[d] += 0.5 * e * Wg[d];
       dtau(tmp, Wp);
-      for (int d = lane; d < D; d += 32) Wq[d] += e * tmp[d];
+      for (int d = lane; d < D; d += TW) Wq[d] += e * tmp[d];
     } else {
-      for (int base = 0; base < D; base += 32 * VCW) {
+      for (int base = 0; base < D; base += TW * VCW) {
         double vp[VCW], vg[VCW], vq[VCW], vm[VCW];
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
-          const int d = base + lane + 32 * j;
+          const int d = base + lane + TW * j;
           const bool ok = d < D;
           vp[j] = ok ? Wp[d] : 0.0;
           vg[j] = ok ? Wg[d] : 0.0;
@@ -374,7 +377,7 @@ struct Chain {
         }
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
-          const int d = base + lane + 32 * j;
+          const int d = base + lane + TW * j;
           if (d < D) {
             const double pn = vp[j] + 0.5 * e * vg[j];
             Wp[d] = pn;
@@ -383,25 +386,25 @@ struct Chain {
         }
       }
     }
-    __syncwarp();
+    tsync<TW>();
   }
   __device__ void complete_leapfrog(double e) {
-    for (int base = 0; base < D; base += 32 * VCW) {
+    for (int base = 0; base < D; base += TW * VCW) {
       double vp[VCW], vg[VCW];
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         vp[j] = d < D ? Wp[d] : 0.0;
         vg[j] = d < D ? Wg[d] : 0.0;
       }
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (d < D) Wp[d] = vp[j] + 0.5 * e * vg[j];
       }
     }
     ++s.n_grad;
-    __syncwarp();
+    tsync<TW>();
   }
   __device__ double energy_W(double* ps) {
     dtau(ps, Wp);
@@ -411,7 +414,7 @@ struct Chain {
     if (p) copy3(Wq, q, Wp, p, Wg, g);
     else copy2(Wq, q, Wg, g);
     s.W_lp = lp;
-    __syncwarp();
+    tsync<TW>();
   }
 
   // ---------------- error / completion ----------------
@@ -431,21 +434,21 @@ struct Chain {
   // draws a candidate into W.q (stream 1), gradient then requested
   __device__ void init_candidate() {
     if (P.has_init) {
-      for (int d = lane; d < D; d += 32) Wq[d] = B.init_q[(size_t)c * P.D + d];
+      for (int d = lane; d < D; d += TW) Wq[d] = B.init_q[(size_t)c * P.D + d];
     } else {
       const uint64_t n0 = s.irng_n;
-      for (int d = lane; d < D; d += 32)
+      for (int d = lane; d < D; d += TW)
         Wq[d] = P.init_radius * (2.0 * rng_uniform(P.seed, chain_id, 1u, n0 + (uint64_t)d) - 1.0);
       s.irng_n = n0 + (uint64_t)D;
     }
     ++s.init_attempts;
     s.phase = PH_INIT;
-    __syncwarp();
+    tsync<TW>();
   }
   __device__ bool W_finite() const {
     bool ok = isfinite(s.W_lp);
-    for (int d = lane; d < D; d += 32) ok = ok && isfinite(Wg[d]);
-    return wall(ok);
+    for (int d = lane; d < D; d += TW) ok = ok && isfinite(Wg[d]);
+    return tall<TW>(ok);
   }
 
   // ---------------- step-size search ----------------
@@ -509,28 +512,28 @@ struct Chain {
       const size_t msz = metric() == 1 ? (size_t)D * D : (size_t)P.D;
       if (metric() == 1) {
         for (int i = 0; i < D; ++i)
-          for (int j = lane; j < D; j += 32) B.out_minv[(size_t)c * msz + (size_t)i * D + j] = minv[(size_t)i * P.ld + j];
+          for (int j = lane; j < D; j += TW) B.out_minv[(size_t)c * msz + (size_t)i * D + j] = minv[(size_t)i * P.ld + j];
       } else {
-        for (int d = lane; d < D; d += 32) B.out_minv[(size_t)c * msz + d] = minv[d];
+        for (int d = lane; d < D; d += TW) B.out_minv[(size_t)c * msz + d] = minv[d];
       }
     }
     s.eps = s.nom_eps;
     if (P.jitter > 0 && !P.replay) s.eps *= 1.0 + P.jitter * (2.0 * uniform() - 1.0);
     load_W_from(Sq, nullptr, Sg, s.S_lp);
     if (P.replay) {
-      for (int d = lane; d < D; d += 32) Wp[d] = B.p0[(size_t)c * P.D + d];
-      __syncwarp();
+      for (int d = lane; d < D; d += TW) Wp[d] = B.p0[(size_t)c * P.D + d];
+      tsync<TW>();
     } else {
       sample_p(Wp);
     }
     dtau(Tsb, Wp);
     s.H0 = kinetic(Wp, Tsb) - s.W_lp;
     s.S_h = s.H0;
-    for (int base = 0; base < D; base += 32 * VCW) {
+    for (int base = 0; base < D; base += TW * VCW) {
       double vp[VCW], vq[VCW], vg[VCW], vs[VCW];
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         const bool ok = d < D;
         vp[j] = ok ? Wp[d] : 0.0;
         vq[j] = ok ? Wq[d] : 0.0;
@@ -539,7 +542,7 @@ struct Chain {
       }
 #pragma unroll
       for (int j = 0; j < VCW; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (d < D) {
           const double p = vp[j];
           Fq[d] = vq[j]; Fp[d] = p; Fg[d] = vg[j];
@@ -557,7 +560,7 @@ struct Chain {
     s.sum_metro = 0;
     s.depth = 0;
     s.divergent = 0;
-    __syncwarp();
+    tsync<TW>();
     return begin_doubling();
   }
 
@@ -602,11 +605,11 @@ struct Chain {
     // any of its stores (the records live in global memory and the compiler
     // cannot reorder loads across possibly aliasing stores).  Masked
     // elements load 0 and add exact zeros to the sums.
-    for (int base = 0; base < D; base += 32 * VCH) {
+    for (int base = 0; base < D; base += TW * VCH) {
       double arho[VCH], brho[VCH], bpb[VCH], ape[VCH], asb[VCH], bse[VCH], bsb[VCH], ase[VCH], bpe[VCH];
 #pragma unroll
       for (int j = 0; j < VCH; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         const bool ok = d < D;
         arho[j] = ok ? Arho[d] : 0.0; brho[j] = ok ? Brho[d] : 0.0; bpb[j] = ok ? Bpb[d] : 0.0;
         ape[j] = ok ? Ape[d] : 0.0;   asb[j] = ok ? Asb[d] : 0.0;   bse[j] = ok ? Bse[d] : 0.0;
@@ -623,7 +626,7 @@ struct Chain {
         s2b += bsb[j] * e1;
         s3a += ase[j] * e2;
         s3b += bse[j] * e2;
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (d < D) {
           Arho[d] = rs;
           Ape[d] = bpe[j];
@@ -633,14 +636,18 @@ struct Chain {
     }
     if (take) copy2(Aq, Bq_, Ag, Bg_);
     if (take && P.diag) copy(rec(A, RV_P), rec(Bk, RV_P));
-    s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
+    {
+      double v6[6] = {s1a, s1b, s2a, s2b, s3a, s3b};
+      tsum_n<TW, 6>(v6);
+      s1a = v6[0]; s1b = v6[1]; s2a = v6[2]; s2b = v6[3]; s3a = v6[4]; s3b = v6[5];
+    }
     if (take) {
       const double lpB = rlp(Bk), hB = rh(Bk);
       rlp(A) = lpB;
       rh(A) = hB;
     }
     rlsw(A) = lsw_sub;
-    __syncwarp();
+    tsync<TW>();
     return (s1b > 0 && s1a > 0) && (s2b > 0 && s2a > 0) && (s3b > 0 && s3a > 0);
   }
 
@@ -661,7 +668,7 @@ struct Chain {
     double vp[VC1], vg[VC1], vq[VC1], vm[VC1];
 #pragma unroll
     for (int j = 0; j < VC1; ++j) {
-      const int d = lane + 32 * j;
+      const int d = lane + TW * j;
       const bool ok = d < D;
       vp[j] = ok ? Wp[d] : 0.0;
       vg[j] = ok ? Wg[d] : 0.0;
@@ -671,7 +678,7 @@ struct Chain {
     double kin = 0;
 #pragma unroll
     for (int j = 0; j < VC1; ++j) {
-      const int d = lane + 32 * j;
+      const int d = lane + TW * j;
       if (d < D) {
         const double p = vp[j] + 0.5 * e * vg[j];
         vp[j] = p;
@@ -683,14 +690,14 @@ struct Chain {
         if (rp) rp[d] = p;
       }
     }
-    double h = 0.5 * wsum(kin) - s.W_lp;
+    double h = 0.5 * tsum<TW>(kin) - s.W_lp;
     if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
     if (h - s.H0 > 1000.0) s.divergent = 1;
     s.sum_metro += (s.H0 - h > 0) ? 1.0 : exp(s.H0 - h);
     rlsw(r) = s.H0 - h;
     rlp(r) = s.W_lp;
     rh(r) = h;
-    __syncwarp();
+    tsync<TW>();
     if (s.divergent) return end_transition();
     if (!(s.leaf & 1) && s.depth != 0) {
       // no pending subtree to merge and the doubling goes on: park the leaf at
@@ -699,14 +706,14 @@ struct Chain {
       ++s.leaf;
 #pragma unroll
       for (int j = 0; j < VC1; ++j) {
-        const int d = lane + 32 * j;
+        const int d = lane + TW * j;
         if (d < D) {
           const double pn = vp[j] + 0.5 * e * vg[j];
           Wp[d] = pn;
           Wq[d] = vq[j] + e * (metric() == 0 ? vm[j] * pn : pn);
         }
       }
-      __syncwarp();
+      tsync<TW>();
       return true;
     }
     return after_leaf(r, e);
@@ -734,7 +741,7 @@ struct Chain {
 
   __device__ bool step_leaf() {
     const double e = s.dir * s.eps;
-    if (metric() != 1 && D <= 32 * VC1) return step_leaf_onepass(e);
+    if (metric() != 1 && D <= TW * VC1) return step_leaf_onepass(e);
     complete_leapfrog(e);
     ++s.n_leapfrog;
     int r = alloc_rec();
@@ -746,8 +753,8 @@ struct Chain {
     double kin = 0;
     if (metric() == 1) {
       dtau(tmp, Wp);
-      for (int d = lane; d < D; d += 32) kin += Wp[d] * tmp[d];
-      for (int d = lane; d < D; d += 32) {
+      for (int d = lane; d < D; d += TW) kin += Wp[d] * tmp[d];
+      for (int d = lane; d < D; d += TW) {
         const double p = Wp[d];
         const double ps = tmp[d];
         pb[d] = p; pe[d] = p; sb[d] = ps; se[d] = ps; rho[d] = p;
@@ -755,11 +762,11 @@ struct Chain {
       }
     } else {
       // the leaf's kinetic energy and its record in one chunked pass
-      for (int base = 0; base < D; base += 32 * VCW) {
+      for (int base = 0; base < D; base += TW * VCW) {
         double vp[VCW], vm[VCW], vq[VCW], vg[VCW];
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
-          const int d = base + lane + 32 * j;
+          const int d = base + lane + TW * j;
           const bool ok = d < D;
           vp[j] = ok ? Wp[d] : 0.0;
           vm[j] = ok && metric() == 0 ? minv[d] : 0.0;
@@ -768,7 +775,7 @@ struct Chain {
         }
 #pragma unroll
         for (int j = 0; j < VCW; ++j) {
-          const int d = base + lane + 32 * j;
+          const int d = base + lane + TW * j;
           if (d < D) {
             const double p = vp[j];
             const double ps = metric() == 0 ? vm[j] * p : p;
@@ -779,14 +786,14 @@ struct Chain {
         }
       }
     }
-    double h = 0.5 * wsum(kin) - s.W_lp;
+    double h = 0.5 * tsum<TW>(kin) - s.W_lp;
     if (isnan(h)) h = __longlong_as_double(0x7ff0000000000000ll);
     if (h - s.H0 > 1000.0) s.divergent = 1;
     s.sum_metro += (s.H0 - h > 0) ? 1.0 : exp(s.H0 - h);
     rlsw(r) = s.H0 - h;
     rlp(r) = s.W_lp;
     rh(r) = h;
-    __syncwarp();
+    tsync<TW>();
     if (s.divergent) return end_transition();
     return after_leaf(r, e);
   }
@@ -824,11 +831,11 @@ struct Chain {
     // backward -> (N reversed, T).
     double s1a = 0, s1b = 0, s2a = 0, s2b = 0, s3a = 0, s3b = 0;
     // loads of a chunk ahead of its stores, as in merge
-    for (int base = 0; base < D; base += 32 * VCH) {
+    for (int base = 0; base < D; base += TW * VCH) {
       double trho[VCH], tpb[VCH], tpe[VCH], tsb[VCH], tse[VCH], nrho[VCH], npb[VCH], npe[VCH], nsb[VCH], nse[VCH];
 #pragma unroll
       for (int j = 0; j < VCH; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         const bool ok = d < D;
         trho[j] = ok ? Trho[d] : 0.0; tpb[j] = ok ? Tpb[d] : 0.0; tpe[j] = ok ? Tpe[d] : 0.0;
         tsb[j] = ok ? Tsb[d] : 0.0;   tse[j] = ok ? Tse[d] : 0.0; nrho[j] = ok ? Nrho[d] : 0.0;
@@ -837,7 +844,7 @@ struct Chain {
       }
 #pragma unroll
       for (int j = 0; j < VCH; ++j) {
-        const int d = base + lane + 32 * j;
+        const int d = base + lane + TW * j;
         if (s.dir > 0) {
           const double rs = trho[j] + nrho[j];
           const double e1 = trho[j] + npb[j];
@@ -857,9 +864,13 @@ struct Chain {
         }
       }
     }
-    s1a = wsum(s1a); s1b = wsum(s1b); s2a = wsum(s2a); s2b = wsum(s2b); s3a = wsum(s3a); s3b = wsum(s3b);
+    {
+      double v6[6] = {s1a, s1b, s2a, s2b, s3a, s3b};
+      tsum_n<TW, 6>(v6);
+      s1a = v6[0]; s1b = v6[1]; s2a = v6[2]; s2b = v6[3]; s3a = v6[4]; s3b = v6[5];
+    }
     free_rec(N);
-    __syncwarp();
+    tsync<TW>();
     bool persist = (s1b > 0 && s1a > 0) && (s2b > 0 && s2a > 0) && (s3b > 0 && s3a > 0);
     if (!persist || s.depth >= P.max_depth) return end_transition();
     return begin_doubling();
@@ -881,7 +892,7 @@ struct Chain {
         dr[0] = s.S_lp; dr[1] = accept; dr[2] = s.eps; dr[3] = s.depth;
         dr[4] = s.n_leapfrog; dr[5] = s.divergent; dr[6] = s.S_h;
       }
-      for (int d = lane; d < D; d += 32) {
+      for (int d = lane; d < D; d += TW) {
         dr[7 + d] = Sq[d];
         dr[7 + P.D + d] = Sp[d];
         dr[7 + 2 * P.D + d] = Sg[d];
@@ -889,11 +900,11 @@ struct Chain {
     }
     if (B.zdraws) {
       double* zr = B.zdraws + ((size_t)c * P.n_saved + s.row) * P.D;
-      for (int d = lane; d < D; d += 32) zr[d] = Sq[d];
+      for (int d = lane; d < D; d += TW) zr[d] = Sq[d];
     } else {
-      warp_write_array(M, Sq, row + 7, lane);
+      warp_write_array<TW>(M, Sq, row + 7, lane);
       // columns past this chain's model (a smaller member of a posterior set)
-      for (int i = M.ncon + lane; i < P.ncon; i += 32) row[7 + i] = __longlong_as_double(0x7ff8000000000000ll);
+      for (int i = M.ncon + lane; i < P.ncon; i += TW) row[7 + i] = __longlong_as_double(0x7ff8000000000000ll);
     }
     ++s.row;
   }
@@ -902,7 +913,7 @@ struct Chain {
   __device__ bool end_transition() {
     const double accept = s.sum_metro / (double)s.n_leapfrog;
     s.n_lf_total += s.n_leapfrog;
-    __syncwarp();
+    tsync<TW>();
     record(accept);
     const bool warm = s.iter < P.num_warmup;
     ++s.iter;
@@ -948,41 +959,41 @@ struct Chain {
     bool ok = true;
     if (metric() == 1) {
       for (int i = 0; i < D; ++i)
-        for (int j = lane; j < D; j += 32) {
+        for (int j = lane; j < D; j += TW) {
           double v = wm2[(size_t)i * P.ld + j] / (n - 1.0);
           v = (n / (n + 5.0)) * v + (i == j ? 1e-3 * (5.0 / (n + 5.0)) : 0.0);
           minv[(size_t)i * P.ld + j] = v;
           ok = ok && isfinite(v);
         }
     } else {
-      for (int d = lane; d < D; d += 32) {
+      for (int d = lane; d < D; d += TW) {
         double v = wm2[d] / (n - 1.0);
         v = (n / (n + 5.0)) * v + 1e-3 * (5.0 / (n + 5.0));
         minv[d] = v;
         ok = ok && isfinite(v);
       }
     }
-    __syncwarp();
-    if (!wall(ok)) { fail(CE_METRIC); return true; }
+    tsync<TW>();
+    if (!tall<TW>(ok)) { fail(CE_METRIC); return true; }
     if (metric() == 1 && !cholesky()) { fail(CE_NOT_PD); return true; }
     // restart the estimator
     s.wf_n = 0;
-    for (int d = lane; d < D; d += 32) wm[d] = 0;
+    for (int d = lane; d < D; d += TW) wm[d] = 0;
     if (metric() == 1) {
       for (int i = 0; i < D; ++i)
-        for (int j = lane; j < D; j += 32) wm2[(size_t)i * P.ld + j] = 0;
+        for (int j = lane; j < D; j += TW) wm2[(size_t)i * P.ld + j] = 0;
     } else {
-      for (int d = lane; d < D; d += 32) wm2[d] = 0;
+      for (int d = lane; d < D; d += TW) wm2[d] = 0;
     }
     ++s.w_counter;
-    __syncwarp();
+    tsync<TW>();
     return true;
   }
 
   __device__ void welford_add() {
     s.wf_n += 1;
     const double n = s.wf_n;
-    for (int d = lane; d < D; d += 32) {
+    for (int d = lane; d < D; d += TW) {
       double q = Sq[d];
       double delta = q - wm[d];
       wm[d] += delta / n;
@@ -990,13 +1001,13 @@ struct Chain {
       else wm2[d] += (q - wm[d]) * delta;
     }
     if (metric() == 1) {
-      __syncwarp();
+      tsync<TW>();
       for (int i = 0; i < D; ++i) {
         double a = Sq[i] - wm[i];
-        for (int j = lane; j < D; j += 32) wm2[(size_t)i * P.ld + j] += a * tmp[j];
+        for (int j = lane; j < D; j += TW) wm2[(size_t)i * P.ld + j] += a * tmp[j];
       }
     }
-    __syncwarp();
+    tsync<TW>();
   }
 
   // Lt (row k holds column k of L) from minv; false if not positive definite
@@ -1011,14 +1022,14 @@ struct Chain {
       double sdiag = minv[(size_t)j * P.ld + j] - t;
       if (!(sdiag > 0)) return false;
       double dj = sqrt(sdiag);
-      for (int i = j + 1 + lane; i < D; i += 32) {
+      for (int i = j + 1 + lane; i < D; i += TW) {
         double u = minv[(size_t)i * P.ld + j];
         for (int k = 0; k < j; ++k) u -= chol[(size_t)k * P.ld + i] * chol[(size_t)k * P.ld + j];
         Lj[i] = u / dj;
       }
       if (lane == 0) Lj[j] = dj;
-      for (int i = lane; i < j; i += 32) Lj[i] = 0.0;
-      __syncwarp();
+      for (int i = lane; i < j; i += TW) Lj[i] = 0.0;
+      tsync<TW>();
     }
     return true;
   }
@@ -1032,7 +1043,7 @@ struct Chain {
           copy(Sg, Wg);
           s.S_lp = s.W_lp;
           ++s.n_grad;
-          __syncwarp();
+          tsync<TW>();
           if (P.adapt) return begin_init_stepsize(0);
           return begin_transition();
         }

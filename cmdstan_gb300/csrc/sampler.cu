@@ -21,6 +21,7 @@
 #include "batched.cuh"
 #include "grad_tc.h"
 #include "grad_wide.h"
+#include "advance.h"
 
 namespace gnuts {
 
@@ -100,31 +101,19 @@ __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, R
 
 // Round mode: advance every live chain by one gradient.  Instantiated per
 // metric (MET), so the diag_e kernel's hot path carries no dense-metric code.
-template <int MET>
-__global__ void __launch_bounds__(128) k_advance(Params P, Bufs B, DevModel M, GradOut G) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= P.C) return;
-  Scal s = B.sc[warp];
-  if (s.phase >= PH_DONE) return;
-  Chain<MET> ch(P, B, M, s, warp, lane);
-  extern __shared__ double gn_cache[];
-  if (P.cache) ch.cache_attach(gn_cache + (size_t)(threadIdx.x >> 5) * P.cache_stride);
-  // gather this chain's gradient from the batched kernel's partial sums
-  s.W_lp = reduce_gradient(G, M, warp, ch.Wq, ch.Wg, lane);
-  __syncwarp();
-  bool more = ch.advance();
-  if (more) stage_request(G, M, warp, ch.Wq, lane);
-  if (P.cache) ch.cache_detach();
-  __syncwarp();
-  if (lane == 0) B.sc[warp] = s;
-}
-
+// k_advance (advance_kind.cu, one object per metric and team width):
+// chains of at least TEAM_MIN_D parameters advance as CTA teams
 static void launch_advance(int blocks, int threads, size_t smem, cudaStream_t st, const Params& P, const Bufs& B,
                            const DevModel& M, const GradOut& G) {
-  if (P.metric == 0) k_advance<0><<<blocks, threads, smem, st>>>(P, B, M, G);
-  else if (P.metric == 1) k_advance<1><<<blocks, threads, smem, st>>>(P, B, M, G);
-  else k_advance<2><<<blocks, threads, smem, st>>>(P, B, M, G);
+  if (M.D >= TEAM_MIN_D && !P.cache) {
+    if (P.metric == 0) advance_launch_k<0, TEAM_TW>(P.C, TEAM_TW, 0, st, P, B, M, G);
+    else if (P.metric == 1) advance_launch_k<1, TEAM_TW>(P.C, TEAM_TW, 0, st, P, B, M, G);
+    else advance_launch_k<2, TEAM_TW>(P.C, TEAM_TW, 0, st, P, B, M, G);
+    return;
+  }
+  if (P.metric == 0) advance_launch_k<0, 32>(blocks, threads, smem, st, P, B, M, G);
+  else if (P.metric == 1) advance_launch_k<1, 32>(blocks, threads, smem, st, P, B, M, G);
+  else advance_launch_k<2, 32>(blocks, threads, smem, st, P, B, M, G);
 }
 
 __global__ void k_log_prob_grad(DevModel M, int n, const double* q, int jac, double* lp, double* g) {
@@ -699,6 +688,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   float total_ms = 0;
   cudaEventElapsedTime(&total_ms, tev[3], tev[4]);
   stats.rounds = (double)rounds;
+  stats.chains_per_cta = M.D >= TEAM_MIN_D && !P.cache ? 1.0 : 4.0;  // launch_advance's choice
   stats.grad_us = nt ? 1e3 * gsum / nt : 0;
   stats.advance_us = nt ? 1e3 * asum / nt : 0;
   stats.device_ms = total_ms;
@@ -781,9 +771,9 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     P.cache = bytes <= 160 * 1024 && !rounds;
     if (P.cache) {
       GN_CUDA(fused_set_smem(m.dev.kind, (int)bytes));
-      GN_CUDA(cudaFuncSetAttribute(k_advance<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-      GN_CUDA(cudaFuncSetAttribute(k_advance<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-      GN_CUDA(cudaFuncSetAttribute(k_advance<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+      GN_CUDA((advance_set_smem_k<0, 32>((int)bytes)));
+      GN_CUDA((advance_set_smem_k<1, 32>((int)bytes)));
+      GN_CUDA((advance_set_smem_k<2, 32>((int)bytes)));
     } else if (!rounds && (size_t)P.cache_stride * sizeof(double) <= 200 * 1024) {
       // large chains: the cache can still hold one or two chains per CTA
       // (the fused-mode autotuner decides whether that pays)

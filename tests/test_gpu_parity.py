@@ -135,6 +135,24 @@ def test_full_run_gaussian_no_adapt_equals_oracle(metric):
     assert np.all(fit.n_grad == ong)
 
 
+def test_team_state_machine_run_equals_oracle():
+    """Chains of at least 512 parameters advance as CTA teams of 128 threads
+    in round mode (the horseshoe workload's D = 2003 runs this way).  An FP64
+    logistic posterior with 520 predictors (D = 521), fixed step size and
+    metric, chains started at zero: the transitions equal the oracle's
+    (tree depth, leapfrog count, divergence) and the draws agree within 1e-8,
+    the team sums differing from the oracle's only in summation order."""
+    data = workloads.logistic(seed=31, N=4096, D=520)
+    gm, om = _pair("logistic", data)
+    kw = dict(num_warmup=0, num_samples=12, seed=77, stepsize=0.01)
+    fit = gm.sample(adapt=False, num_chains=4, chain_id=1, inits=np.zeros(gm.dim), **kw)
+    od, _, _, ong = om.run_chains(4, threads=4, first_chain_id=1, inits=np.zeros(gm.dim), adapt_engaged=0, **kw)
+    assert fit.timing["chains_per_cta"] == 1.0  # one chain per CTA: the team path ran
+    np.testing.assert_array_equal(fit.draws[:, :, 3:6], od[:, :, 3:6])
+    np.testing.assert_allclose(fit.draws, od, rtol=1e-8, atol=1e-9)
+    assert np.all(fit.n_grad == ong)
+
+
 @pytest.mark.parametrize("metric", ["diag_e", "dense_e", "unit_e"])
 def test_adaptive_run_starts_identical_to_oracle(metric):
     """With adaptation on, ulp differences of libm vs CUDA math are amplified

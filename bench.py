@@ -366,7 +366,27 @@ def bench_horseshoe(peaks, chains=256):
     with ThreadPoolExecutor(threads) as ex:
         list(ex.map(lambda i: om.log_prob_grad(q[i], True), range(threads)))
     cw = time.perf_counter() - t
-    return {"workload": "horseshoe logistic N=200000 x K=1000 (D=2003), %d chains, diag_e, 30 warmup + 10 draws "
+    # dense_e arm: per-chain 2003 x 2003 metrics (FP32 metric product and
+    # momentum solve in each chain's team).  Sampling only, at the diag_e
+    # run's median step size with the identity as the metric: the dense
+    # machinery's cost per gradient.  (The adaptive windows add a
+    # D x D Welford update per transition and an FP64 Cholesky per window
+    # end; a 30 + 10 adaptive run of the same chains took 386 s.)
+    eps_med = float(np.median(fit.stepsize))
+    t = time.perf_counter()
+    fd = m.sample(metric="dense_e", adapt=False, num_chains=chains, num_warmup=0, num_samples=10, seed=4,
+                  stepsize=eps_med, precision=gn.PRECISION_MIXED, refresh=0)
+    dense_wall = time.perf_counter() - t
+    tmd = fd.timing
+    dense = {"workload": "same model and chains, dense_e (identity metric), no adaptation, 10 draws at the diag_e "
+                         "run's median step size (bounded sample)",
+             "grad_evals_per_s": float(fd.n_leapfrog.sum()) / (float(tmd["device_ms"]) / 1e3),
+             "device_s": float(tmd["device_ms"]) / 1e3, "wall_s": dense_wall, "leapfrogs": float(fd.n_leapfrog.sum()),
+             "kernels_us": {"wide_gradient": float(tmd["grad_kernel_us"]), "k_advance": float(tmd["advance_kernel_us"])},
+             "finite_draws": bool(np.all(np.isfinite(fd.draws[:, :, :7])))}
+    del fd
+    return {"dense_e": dense,
+            "workload": "horseshoe logistic N=200000 x K=1000 (D=2003), %d chains, diag_e, 30 warmup + 10 draws "
                         "(bounded sample), mixed precision" % chains,
             "grad_evals_per_s": grads / dev_s, "device_s": dev_s, "leapfrogs": grads,
             "kernels_us": {"wide_gradient": g_us, "k_advance": float(tm["advance_kernel_us"])},

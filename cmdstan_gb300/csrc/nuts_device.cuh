@@ -68,7 +68,12 @@ struct Params {
   int cache_stride;   // doubles of shared memory per warp when cached
   int diag;           // diagnostic rows wanted: track the selected point's momentum
   int nrv;            // vectors per subtree record: 7, or 8 with diag (proposal momentum)
+  int dense32;        // dense metric of a team-mode chain on the mixed path: metric
+                      // product, momentum draw and Welford covariance in FP32
 };
+
+// largest D of the FP32 dense path (its vectors are staged in shared memory)
+constexpr int DENSE32_MAXD = 2048;
 
 // vectors cached per chain (diag / unit metric also caches minv, wm, wm2)
 constexpr int NCACHE_VEC = 17;
@@ -97,6 +102,8 @@ struct Bufs {
   double* zdraws;        // [C][n_saved][D]: sampler-space draws (flow runs; write_array happens later)
   double* Sp;            // [C][ld] momentum of the selected point (diag)
   double* diag_draws;    // [C][n_saved][7 + 3D]: sampler columns, q, p, gradient (diag)
+  float *minv32, *chol32;          // dense32: FP32 copies of minv and chol [C][D][ld]
+  float *wm2_32, *wm2_32lo;         // dense32: Welford sums as float-float pairs (hi, lo) [C][D][ld]
   Scal* sc;
   int* done_count;
 };
@@ -132,6 +139,7 @@ struct Chain {
   double *Wq, *Wp, *Wg, *Fq, *Fp, *Fg, *Bq, *Bp, *Bg, *Sq, *Sg, *Tpb, *Tsb, *Tpe, *Tse, *Trho;
   double *minv, *chol, *wm, *wm2, *tmp;
   double* Sp;   // momentum of the selected point (diagnostic rows only)
+  float *m32 = nullptr, *l32 = nullptr, *w32 = nullptr, *w32lo = nullptr;  // dense32 matrices of this chain
   double* rsc;  // this chain's record scalars [R][3]
   double* cache_base = nullptr;
 
@@ -152,6 +160,20 @@ struct Chain {
     wm = b.wm + o;
     wm2 = b.wm2 + mo;
     Sp = b.Sp ? b.Sp + o : nullptr;
+    if (TW > 32 && p.dense32) {
+      m32 = b.minv32 + mo;
+      l32 = b.chol32 + mo;
+      w32 = b.wm2_32 + mo;
+      w32lo = b.wm2_32lo + mo;
+    }
+  }
+  __device__ __forceinline__ bool dense32() const { return TW > 32 && MET != 0 && MET != 2 && m32 != nullptr; }
+  // the team's FP32 staging vectors (shared memory, four of DENSE32_MAXD;
+  // the dense32 steps that use them -- metric product, momentum solve,
+  // Welford update -- never overlap)
+  static __device__ __forceinline__ float* fbuf() {
+    __shared__ float b[4 * DENSE32_MAXD];
+    return b;
   }
   __device__ __forceinline__ int metric() const { return MET >= 0 ? MET : P.metric; }
   __device__ double* rec(int r, int v) const {
@@ -319,6 +341,8 @@ struct Chain {
           if (d < D) out[d] = metric() == 0 ? vm[j] * vp[j] : vp[j];
         }
       }
+    } else if (dense32()) {
+      dtau32(out, p);
     } else {
       tsync<TW>();
       for (int d = lane; d < D; d += TW) {
@@ -328,12 +352,44 @@ struct Chain {
       }
     }
   }
+  // dense32 metric product: p staged in FP32 in shared memory, thread l
+  // forms outputs l, l + TW, ... (16 per pass) from rows of the symmetric
+  // FP32 minv, accumulating in FP32 in row order
+  __device__ void dtau32(double* out, const double* p) const {
+    float* ps = fbuf();
+    tsync<TW>();
+    for (int d = lane; d < D; d += TW) ps[d] = (float)p[d];
+    tsync<TW>();
+    constexpr int NO = 16;
+    for (int d0 = 0; d0 < D; d0 += TW * NO) {
+      float acc[NO];
+#pragma unroll
+      for (int k = 0; k < NO; ++k) acc[k] = 0.f;
+      const float* col = m32 + d0 + lane;
+      const int nk = min(NO, (D - d0 - lane + TW - 1) / TW);  // outputs of this thread in the pass
+#pragma unroll 2
+      for (int j = 0; j < D; ++j) {
+        const float pj = ps[j];
+        const float* row = col + (size_t)j * P.ld;
+#pragma unroll
+        for (int k = 0; k < NO; ++k)
+          if (k < nk) acc[k] = fmaf(row[TW * k], pj, acc[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < NO; ++k)
+        if (k < nk) out[d0 + lane + TW * k] = (double)acc[k];
+    }
+    tsync<TW>();
+  }
   // kinetic energy 0.5 p.(minv p), using a precomputed ps = minv p
   __device__ double kinetic(const double* p, const double* ps) const { return 0.5 * dot(p, ps); }
 
   __device__ void sample_p(double* p) {
     const uint64_t n0 = s.rng_n;
-    if (metric() == 1) {
+    if (dense32()) {
+      for (int d = lane; d < D; d += TW) tmp[d] = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
+      solve_lt32(p);
+    } else if (metric() == 1) {
       for (int d = lane; d < D; d += TW) tmp[d] = rng_normal(P.seed, chain_id, 0u, n0 + (uint64_t)(d >> 1), d & 1);
       tsync<TW>();
       // solve Lt p = z, back substitution over rows of Lt (Lt[i][k] = L[k][i])
@@ -356,6 +412,69 @@ struct Chain {
     tsync<TW>();
   }
   __device__ double uniform() { return rng_uniform(P.seed, chain_id, 0u, s.rng_n++); }
+
+  // dense32 momentum: solve Lt p = z (z in tmp) in FP32, 32 rows per block
+  // from the bottom.  For block [i0, i0 + 32) the team first forms each row's
+  // sum over the solved entries k >= i0 + 32 (thread t takes k = i0 + 32 + t,
+  // + TW, ...; a warp reduce-scatter leaves row i0 + l's sum with lane l, and
+  // the warps' sums are added in warp order), then warp 0 solves the 32 x 32
+  // triangle with shuffles.
+  __device__ void solve_lt32(double* p) {
+    float* ps = fbuf();
+    __shared__ float red[TW / 32][32];
+    const int wid = lane >> 5, ln = lane & 31;
+    tsync<TW>();
+    for (int i1 = D; i1 > 0; i1 -= 32) {
+      const int i0 = max(0, i1 - 32), nb = i1 - i0;
+      float acc[32];
+#pragma unroll
+      for (int r = 0; r < 32; ++r) acc[r] = 0.f;
+      for (int k = i1 + lane; k < D; k += TW) {
+        const float pk = ps[k];
+#pragma unroll
+        for (int r = 0; r < 32; ++r)
+          if (r < nb) acc[r] = fmaf(l32[(size_t)(i0 + r) * P.ld + k], pk, acc[r]);
+      }
+      // reduce-scatter over the warp: after the five steps lane l holds row l
+#pragma unroll
+      for (int h = 16; h >= 1; h >>= 1) {
+        const bool upper = (ln & h) != 0;
+#pragma unroll
+        for (int r = 0; r < h; ++r) {
+          const float send = upper ? acc[r] : acc[r + h];
+          const float keep = upper ? acc[r + h] : acc[r];
+          acc[r] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+      }
+      if constexpr (TW > 32) {
+        red[wid][ln] = acc[0];
+        tsync<TW>();
+      }
+      if (wid == 0) {
+        float rsum = 0.f;
+        if constexpr (TW > 32) {
+#pragma unroll
+          for (int w = 0; w < TW / 32; ++w) rsum += red[w][ln];
+        } else {
+          rsum = acc[0];
+        }
+        // row i0 + ln: (z - rsum - sum over the block's later rows) / diagonal
+        float v = ln < nb ? (float)tmp[i0 + ln] - rsum : 0.f;
+        const float* row = l32 + (size_t)(i0 + (ln < nb ? ln : 0)) * P.ld;
+        for (int r = nb - 1; r >= 0; --r) {
+          float pr = 0.f;
+          if (ln == r) pr = v / row[i0 + r];
+          pr = __shfl_sync(0xffffffffu, pr, r);
+          if (ln < r) v = fmaf(-row[i0 + r], pr, v);
+          if (ln == r) {
+            ps[i0 + r] = pr;
+            p[i0 + r] = (double)pr;
+          }
+        }
+      }
+      tsync<TW>();
+    }
+  }
 
   // W.p += e/2 g ; W.q += e * minv W.p   (gradient at W.q then requested)
   __device__ void begin_leapfrog(double e) {
@@ -960,9 +1079,11 @@ struct Chain {
     if (metric() == 1) {
       for (int i = 0; i < D; ++i)
         for (int j = lane; j < D; j += TW) {
-          double v = wm2[(size_t)i * P.ld + j] / (n - 1.0);
+          const size_t ij = (size_t)i * P.ld + j;
+          double v = (dense32() ? (double)w32[ij] + (double)w32lo[ij] : wm2[ij]) / (n - 1.0);
           v = (n / (n + 5.0)) * v + (i == j ? 1e-3 * (5.0 / (n + 5.0)) : 0.0);
-          minv[(size_t)i * P.ld + j] = v;
+          minv[ij] = v;
+          if (dense32()) m32[ij] = (float)v;
           ok = ok && isfinite(v);
         }
     } else {
@@ -976,10 +1097,17 @@ struct Chain {
     tsync<TW>();
     if (!tall<TW>(ok)) { fail(CE_METRIC); return true; }
     if (metric() == 1 && !cholesky()) { fail(CE_NOT_PD); return true; }
+    if (dense32()) copy_chol32();
     // restart the estimator
     s.wf_n = 0;
     for (int d = lane; d < D; d += TW) wm[d] = 0;
-    if (metric() == 1) {
+    if (dense32()) {
+      for (int i = 0; i < D; ++i)
+        for (int j = lane; j < D; j += TW) {
+          w32[(size_t)i * P.ld + j] = 0.f;
+          w32lo[(size_t)i * P.ld + j] = 0.f;
+        }
+    } else if (metric() == 1) {
       for (int i = 0; i < D; ++i)
         for (int j = lane; j < D; j += TW) wm2[(size_t)i * P.ld + j] = 0;
     } else {
@@ -1000,7 +1128,45 @@ struct Chain {
       if (metric() == 1) tmp[d] = delta;
       else wm2[d] += (q - wm[d]) * delta;
     }
-    if (metric() == 1) {
+    if (dense32()) {
+      // wm2 += a b^T with a = q - mean (updated), b = q - mean (previous), in
+      // float-float arithmetic (about 44 significant bits): an FP32 sum's
+      // rounding, relative to the large variances of a wide posterior, can
+      // exceed the 1e-3 (5 / (n + 5)) ridge of a short window and leave the
+      // estimate indefinite.  Products are split exactly (two-product) and
+      // added with a two-sum.
+      float* bh = fbuf();
+      float* bl = bh + DENSE32_MAXD;
+      float* ah = bh + 2 * DENSE32_MAXD;
+      float* al = bh + 3 * DENSE32_MAXD;
+      tsync<TW>();
+      for (int d = lane; d < D; d += TW) {
+        const double b = tmp[d], a = Sq[d] - wm[d];
+        const float hb = (float)b, ha = (float)a;
+        bh[d] = hb;
+        bl[d] = (float)(b - (double)hb);
+        ah[d] = ha;
+        al[d] = (float)(a - (double)ha);
+      }
+      tsync<TW>();
+      for (int i = 0; i < D; ++i) {
+        const float a0 = ah[i], a1 = al[i];
+        float* wr = w32 + (size_t)i * P.ld;
+        float* wl = w32lo + (size_t)i * P.ld;
+        for (int j = lane; j < D; j += TW) {
+          const float b0 = bh[j], b1 = bl[j];
+          const float pr = a0 * b0;
+          const float pe = fmaf(a0, b1, fmaf(a1, b0, fmaf(a0, b0, -pr)));
+          const float hi = wr[j];
+          const float sm = hi + pr;
+          const float bv = sm - hi;
+          const float t = ((hi - (sm - bv)) + (pr - bv)) + (wl[j] + pe);
+          const float nh = sm + t;
+          wr[j] = nh;
+          wl[j] = t - (nh - sm);
+        }
+      }
+    } else if (metric() == 1) {
       tsync<TW>();
       for (int i = 0; i < D; ++i) {
         double a = Sq[i] - wm[i];
@@ -1015,9 +1181,19 @@ struct Chain {
     for (int j = 0; j < D; ++j) {
       double* Lj = chol + (size_t)j * P.ld;  // Lt row j = L column j
       double t = 0;
-      for (int k = 0; k < j; ++k) {
-        double l = chol[(size_t)k * P.ld + j];
-        t += l * l;
+      if constexpr (TW > 32) {
+        // a team sums the column's squares in parallel (one warp keeps the
+        // serial order, as the reference's factorisation does)
+        for (int k = lane; k < j; k += TW) {
+          const double l = chol[(size_t)k * P.ld + j];
+          t += l * l;
+        }
+        t = tsum<TW>(t);
+      } else {
+        for (int k = 0; k < j; ++k) {
+          double l = chol[(size_t)k * P.ld + j];
+          t += l * l;
+        }
       }
       double sdiag = minv[(size_t)j * P.ld + j] - t;
       if (!(sdiag > 0)) return false;
@@ -1032,6 +1208,11 @@ struct Chain {
       tsync<TW>();
     }
     return true;
+  }
+  __device__ void copy_chol32() {
+    for (int i = 0; i < D; ++i)
+      for (int j = lane; j < D; j += TW) l32[(size_t)i * P.ld + j] = (float)chol[(size_t)i * P.ld + j];
+    tsync<TW>();
   }
 
   // ---------------- driver ----------------

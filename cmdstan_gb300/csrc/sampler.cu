@@ -70,20 +70,38 @@ __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, R
   }
   const int D = P.D;
   if (P.metric == 1) {
+    const size_t mo = (size_t)warp * D * P.ld;
     for (int i = 0; i < D; ++i)
       for (int j = lane; j < D; j += 32) {
         double v = inv_metric ? inv_metric[((size_t)warp * D + i) * D + j] : (i == j ? 1.0 : 0.0);
         ch.minv[(size_t)i * P.ld + j] = v;
         ch.wm2[(size_t)i * P.ld + j] = 0.0;
+        if (P.dense32) {
+          B.minv32[mo + (size_t)i * P.ld + j] = (float)v;
+          B.wm2_32[mo + (size_t)i * P.ld + j] = 0.f;
+          B.wm2_32lo[mo + (size_t)i * P.ld + j] = 0.f;
+        }
       }
     __syncwarp();
-    if (!ch.cholesky()) {
+    bool pd = true;
+    if (inv_metric) {
+      pd = ch.cholesky();
+    } else {
+      // the factor of the identity is the identity (what cholesky() computes, bit for bit)
+      for (int i = 0; i < D; ++i)
+        for (int j = lane; j < D; j += 32) ch.chol[(size_t)i * P.ld + j] = i == j ? 1.0 : 0.0;
+      __syncwarp();
+    }
+    if (!pd) {
       s.err = CE_NOT_PD;
       s.phase = PH_ERROR;
       if (lane == 0) atomicAdd(B.done_count, 1);
       if (lane == 0) B.sc[warp] = s;
       return;
     }
+    if (P.dense32)
+      for (int i = 0; i < D; ++i)
+        for (int j = lane; j < D; j += 32) B.chol32[mo + (size_t)i * P.ld + j] = (float)ch.chol[(size_t)i * P.ld + j];
   } else {
     for (int d = lane; d < D; d += 32) {
       ch.minv[d] = (P.metric == 0 && inv_metric) ? inv_metric[(size_t)warp * D + d] : 1.0;
@@ -780,6 +798,10 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
       const size_t one = (size_t)P.cache_stride * sizeof(double);
       GN_CUDA(fused_set_smem(m.dev.kind, (int)std::min<size_t>(2 * one <= 200 * 1024 ? 2 * one : one, 200 * 1024)));
     }
+    // a wide dense-metric chain on the mixed path: its team does the metric
+    // product, momentum draw and covariance updates in FP32
+    P.dense32 = rc.metric == 1 && rounds && !P.cache && a.precision == GNUTS_PRECISION_MIXED && D >= TEAM_MIN_D &&
+                D <= DENSE32_MAXD;
   }
 
   Arena ar;
@@ -798,6 +820,12 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
   GN_CUDA(ar.alloc(&B.minv, mat));
   GN_CUDA(ar.alloc(&B.wm2, mat));
   if (P.metric == 1) GN_CUDA(ar.alloc(&B.chol, mat));
+  if (P.dense32) {
+    GN_CUDA(ar.alloc(&B.minv32, mat));
+    GN_CUDA(ar.alloc(&B.chol32, mat));
+    GN_CUDA(ar.alloc(&B.wm2_32, mat));
+    GN_CUDA(ar.alloc(&B.wm2_32lo, mat));
+  }
   GN_CUDA(ar.alloc(&B.draws, (size_t)C * P.n_saved * P.ncol));
   GN_CUDA(ar.alloc(&B.out_eps, C));
   const size_t msz = P.metric == 1 ? (size_t)D * D : (size_t)D;

@@ -104,6 +104,8 @@ struct Bufs {
   double* diag_draws;    // [C][n_saved][7 + 3D]: sampler columns, q, p, gradient (diag)
   float *minv32, *chol32;          // dense32: FP32 copies of minv and chol [C][D][ld]
   float *wm2_32, *wm2_32lo;         // dense32: Welford sums as float-float pairs (hi, lo) [C][D][ld]
+  float* wpend;   // dense32: a pending Welford sample per chain [C][4][ld]: b hi, b lo, a hi, a lo
+  int* wlist;     // dense32: [0] pending count, [1] finished-CTA count, [2 + k] chain ids
   Scal* sc;
   int* done_count;
 };
@@ -128,6 +130,21 @@ __device__ __forceinline__ double lse(double a, double b) {
 // MET >= 0 fixes the metric at compile time (0 diag_e, 1 dense_e, 2 unit_e):
 // a kernel instantiated per metric carries only that metric's code on its
 // hot path; MET = -1 reads it from the run's parameters.
+// float-float accumulation (hi, lo) += (a0 + a1) (b0 + b1): the product of
+// the leading parts split exactly (two-product), the cross terms added to its
+// error, the sum formed with a two-sum and renormalised
+__device__ __forceinline__ void ff_axpy(float& hi_io, float& lo_io, float a0, float a1, float b0, float b1) {
+  const float pr = a0 * b0;
+  const float pe = fmaf(a0, b1, fmaf(a1, b0, fmaf(a0, b0, -pr)));
+  const float hi = hi_io;
+  const float sm = hi + pr;
+  const float bv = sm - hi;
+  const float t = ((hi - (sm - bv)) + (pr - bv)) + (lo_io + pe);
+  const float nh = sm + t;
+  hi_io = nh;
+  lo_io = t - (nh - sm);
+}
+
 template <int MET = -1, int TW = 32>
 struct Chain {
   const Params& P;
@@ -352,32 +369,44 @@ struct Chain {
       }
     }
   }
-  // dense32 metric product: p staged in FP32 in shared memory, thread l
-  // forms outputs l, l + TW, ... (16 per pass) from rows of the symmetric
-  // FP32 minv, accumulating in FP32 in row order
+  // dense32 metric product: p staged in FP32 in shared memory; thread l
+  // forms outputs 4l .. 4l + 3 of each group of 4 TW (four groups per pass)
+  // from 16-byte loads of rows of the symmetric FP32 minv (ld is a multiple
+  // of 4, so the loads are aligned and stay inside the row's padding),
+  // accumulating in FP32 in row order
   __device__ void dtau32(double* out, const double* p) const {
     float* ps = fbuf();
     tsync<TW>();
     for (int d = lane; d < D; d += TW) ps[d] = (float)p[d];
     tsync<TW>();
-    constexpr int NO = 16;
-    for (int d0 = 0; d0 < D; d0 += TW * NO) {
-      float acc[NO];
+    constexpr int NG = 4;
+    for (int d0 = 0; d0 < D; d0 += 4 * TW * NG) {
+      float4 acc[NG];
 #pragma unroll
-      for (int k = 0; k < NO; ++k) acc[k] = 0.f;
-      const float* col = m32 + d0 + lane;
-      const int nk = min(NO, (D - d0 - lane + TW - 1) / TW);  // outputs of this thread in the pass
+      for (int g = 0; g < NG; ++g) acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const int db = d0 + 4 * lane;
 #pragma unroll 2
       for (int j = 0; j < D; ++j) {
         const float pj = ps[j];
-        const float* row = col + (size_t)j * P.ld;
+        const float4* row = reinterpret_cast<const float4*>(m32 + (size_t)j * P.ld + db);
 #pragma unroll
-        for (int k = 0; k < NO; ++k)
-          if (k < nk) acc[k] = fmaf(row[TW * k], pj, acc[k]);
+        for (int g = 0; g < NG; ++g)
+          if (db + 4 * TW * g < D) {
+            const float4 m = row[TW * g];
+            acc[g].x = fmaf(m.x, pj, acc[g].x);
+            acc[g].y = fmaf(m.y, pj, acc[g].y);
+            acc[g].z = fmaf(m.z, pj, acc[g].z);
+            acc[g].w = fmaf(m.w, pj, acc[g].w);
+          }
       }
 #pragma unroll
-      for (int k = 0; k < NO; ++k)
-        if (k < nk) out[d0 + lane + TW * k] = (double)acc[k];
+      for (int g = 0; g < NG; ++g) {
+        const int d = db + 4 * TW * g;
+        const float v[4] = {acc[g].x, acc[g].y, acc[g].z, acc[g].w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (d + e < D) out[d + e] = (double)v[e];
+      }
     }
     tsync<TW>();
   }
@@ -1059,8 +1088,8 @@ struct Chain {
   // windowed Welford adaptation; returns true when the metric was updated
   __device__ bool learn_metric() {
     const bool in_window = s.w_counter >= s.w_ib && s.w_counter < s.w_nw - s.w_tb && s.w_counter != s.w_nw;
-    if (in_window) welford_add();
     const bool end_window = s.w_counter == s.w_next && s.w_counter != s.w_nw;
+    if (in_window) welford_add(end_window);  // a window end reads the estimate next
     if (!end_window) {
       ++s.w_counter;
       return false;
@@ -1118,7 +1147,7 @@ struct Chain {
     return true;
   }
 
-  __device__ void welford_add() {
+  __device__ void welford_add(bool local) {
     s.wf_n += 1;
     const double n = s.wf_n;
     for (int d = lane; d < D; d += TW) {
@@ -1133,12 +1162,15 @@ struct Chain {
       // float-float arithmetic (about 44 significant bits): an FP32 sum's
       // rounding, relative to the large variances of a wide posterior, can
       // exceed the 1e-3 (5 / (n + 5)) ridge of a short window and leave the
-      // estimate indefinite.  Products are split exactly (two-product) and
-      // added with a two-sum.
-      float* bh = fbuf();
-      float* bl = bh + DENSE32_MAXD;
-      float* ah = bh + 2 * DENSE32_MAXD;
-      float* al = bh + 3 * DENSE32_MAXD;
+      // estimate indefinite.  a and b are split into float pairs; the D x D
+      // update is applied here at a window end (the estimate is read next),
+      // otherwise queued for k_welford_dense, which runs the round's queued
+      // updates over every SM instead of this chain's one.
+      float* bh = local ? fbuf() : B.wpend + (size_t)c * 4 * P.ld;
+      const int st = local ? DENSE32_MAXD : P.ld;
+      float* bl = bh + st;
+      float* ah = bh + 2 * st;
+      float* al = bh + 3 * st;
       tsync<TW>();
       for (int d = lane; d < D; d += TW) {
         const double b = tmp[d], a = Sq[d] - wm[d];
@@ -1149,22 +1181,16 @@ struct Chain {
         al[d] = (float)(a - (double)ha);
       }
       tsync<TW>();
-      for (int i = 0; i < D; ++i) {
-        const float a0 = ah[i], a1 = al[i];
-        float* wr = w32 + (size_t)i * P.ld;
-        float* wl = w32lo + (size_t)i * P.ld;
-        for (int j = lane; j < D; j += TW) {
-          const float b0 = bh[j], b1 = bl[j];
-          const float pr = a0 * b0;
-          const float pe = fmaf(a0, b1, fmaf(a1, b0, fmaf(a0, b0, -pr)));
-          const float hi = wr[j];
-          const float sm = hi + pr;
-          const float bv = sm - hi;
-          const float t = ((hi - (sm - bv)) + (pr - bv)) + (wl[j] + pe);
-          const float nh = sm + t;
-          wr[j] = nh;
-          wl[j] = t - (nh - sm);
+      if (local) {
+        for (int i = 0; i < D; ++i) {
+          const float a0 = ah[i], a1 = al[i];
+          float* wr = w32 + (size_t)i * P.ld;
+          float* wl = w32lo + (size_t)i * P.ld;
+          for (int j = lane; j < D; j += TW) ff_axpy(wr[j], wl[j], a0, a1, bh[j], bl[j]);
         }
+      } else if (lane == 0) {
+        const int k = atomicAdd(B.wlist, 1);
+        B.wlist[2 + k] = c;
       }
     } else if (metric() == 1) {
       tsync<TW>();

@@ -119,6 +119,50 @@ __global__ void k_init(Params P, Bufs B, DevModel M, const double* inv_metric, R
 
 // Round mode: advance every live chain by one gradient.  Instantiated per
 // metric (MET), so the diag_e kernel's hot path carries no dense-metric code.
+// The Welford samples that this round's k_advance queued for wide dense
+// chains (Chain::welford_add): item = (queued chain, 16 rows of its D x D
+// float-float sums), spread over every SM.  The last CTA to finish empties
+// the queue for the next round.
+constexpr int WF_THREADS = 256, WF_ROWS = 16;
+__global__ void __launch_bounds__(WF_THREADS) k_welford_dense(Params P, Bufs B) {
+  const int n = B.wlist[0];
+  const int D = P.D, nrb = (D + WF_ROWS - 1) / WF_ROWS;
+  for (int it = blockIdx.x; it < n * nrb; it += gridDim.x) {
+    const int c = B.wlist[2 + it / nrb], i0 = (it % nrb) * WF_ROWS;
+    const float* bh = B.wpend + (size_t)c * 4 * P.ld;
+    const float *bl = bh + P.ld, *ah = bh + 2 * P.ld, *al = bh + 3 * P.ld;
+    const size_t mo = (size_t)c * D * P.ld;
+    // 16-byte vectors (ld is a multiple of 4; the padding columns of b are
+    // zero, so the padding of a row's sums stays zero)
+    for (int i = i0; i < min(D, i0 + WF_ROWS); ++i) {
+      const float a0 = ah[i], a1 = al[i];
+      float4* wr = reinterpret_cast<float4*>(B.wm2_32 + mo + (size_t)i * P.ld);
+      float4* wl = reinterpret_cast<float4*>(B.wm2_32lo + mo + (size_t)i * P.ld);
+      const float4* b0 = reinterpret_cast<const float4*>(bh);
+      const float4* b1 = reinterpret_cast<const float4*>(bl);
+      for (int j = threadIdx.x; 4 * j < D; j += WF_THREADS) {
+        float4 h = wr[j], l = wl[j];
+        const float4 x = b0[j], y = b1[j];
+        ff_axpy(h.x, l.x, a0, a1, x.x, y.x);
+        ff_axpy(h.y, l.y, a0, a1, x.y, y.y);
+        ff_axpy(h.z, l.z, a0, a1, x.z, y.z);
+        ff_axpy(h.w, l.w, a0, a1, x.w, y.w);
+        wr[j] = h;
+        wl[j] = l;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&B.wlist[1], 1) == (int)gridDim.x - 1) {
+      B.wlist[0] = 0;
+      B.wlist[1] = 0;
+      __threadfence();
+    }
+  }
+}
+
 // k_advance (advance_kind.cu, one object per metric and team width):
 // chains of at least TEAM_MIN_D parameters advance as CTA teams
 static void launch_advance(int blocks, int threads, size_t smem, cudaStream_t st, const Params& P, const Bufs& B,
@@ -619,6 +663,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   for (int r = 0; r < ROUNDS; ++r) {
     glm_rc |= launch_glm(G, M, stream);
     launch_advance(blocks, threads, cache_bytes(P), stream, P, B, M, G);
+    if (P.dense32) k_welford_dense<<<2 * 152, WF_THREADS, 0, stream>>>(P, B);
   }
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
   if (glm_rc) {
@@ -653,13 +698,14 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
       }
       GN_CUDA(cudaEventRecord(tev[1], stream));
       launch_advance(blocks, threads, cache_bytes(P), stream, P, B, M, G);
+      if (P.dense32) k_welford_dense<<<2 * 152, WF_THREADS, 0, stream>>>(P, B);
       GN_CUDA(cudaEventRecord(tev[2], stream));
       rounds += 1;
-      launches += 2;
+      launches += P.dense32 ? 3 : 2;
     } else {
       GN_CUDA(cudaGraphLaunch(exec, stream));
       rounds += ROUNDS;
-      launches += 2 * ROUNDS;
+      launches += (P.dense32 ? 3 : 2) * ROUNDS;
     }
     GN_CUDA(cudaMemcpyAsync(&h_done[b], B.done_count, sizeof(int), cudaMemcpyDeviceToHost, stream));
     if ((st = streamer.request_rows(stream, b, err))) return st;
@@ -825,6 +871,8 @@ static int run_nuts_impl(Model& m, const gnuts_sample_args& a, const RunConfig& 
     GN_CUDA(ar.alloc(&B.chol32, mat));
     GN_CUDA(ar.alloc(&B.wm2_32, mat));
     GN_CUDA(ar.alloc(&B.wm2_32lo, mat));
+    GN_CUDA(ar.alloc(&B.wpend, vec * 4));
+    GN_CUDA(ar.alloc(&B.wlist, (size_t)C + 2));
   }
   GN_CUDA(ar.alloc(&B.draws, (size_t)C * P.n_saved * P.ncol));
   GN_CUDA(ar.alloc(&B.out_eps, C));

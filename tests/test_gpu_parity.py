@@ -153,6 +153,29 @@ def test_team_state_machine_run_equals_oracle():
     assert np.all(fit.n_grad == ong)
 
 
+def test_team_dense_fp64_run_equals_oracle():
+    """The team path with an FP64 dense metric (D = 521: team metric product,
+    back substitution with team sums per row, the initial Cholesky factor of a
+    given SPD inverse metric computed by the warp that initialises the
+    chain), fixed step size: the transitions equal the oracle's and the draws
+    agree within 1e-8."""
+    data = workloads.logistic(seed=32, N=4096, D=520)
+    gm, om = _pair("logistic", data)
+    D = gm.dim
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((D, D)) * (0.3 / np.sqrt(D))
+    im = (A @ A.T + np.eye(D)) * 1e-3  # about the posterior scale: sd ~ 0.03
+    kw = dict(num_warmup=0, num_samples=6, seed=78, stepsize=0.2)
+    fit = gm.sample(metric="dense_e", adapt=False, num_chains=4, chain_id=1, inits=np.zeros(D),
+                    inv_metric=im.ravel(), **kw)
+    od, _, _, ong = om.run_chains(4, threads=4, first_chain_id=1, inits=np.zeros(D), metric=1, adapt_engaged=0,
+                                  inv_metric=im.ravel(), **kw)
+    assert fit.timing["chains_per_cta"] == 1.0
+    np.testing.assert_array_equal(fit.draws[:, :, 3:6], od[:, :, 3:6])
+    np.testing.assert_allclose(fit.draws, od, rtol=1e-8, atol=1e-9)
+    assert np.all(fit.n_grad == ong)
+
+
 def test_dense_metric_team_fp32_matches_fp64():
     """dense_e on the mixed path for a chain of at least 512 parameters: its
     team forms M^-1 p from an FP32 copy of the metric, draws the momentum by a

@@ -184,7 +184,8 @@ struct Chain {
       w32lo = b.wm2_32lo + mo;
     }
   }
-  __device__ __forceinline__ bool dense32() const { return TW > 32 && MET != 0 && MET != 2 && m32 != nullptr; }
+  // only the round-mode team kernel of the dense metric (MET = 1) carries this code
+  __device__ __forceinline__ bool dense32() const { return TW > 32 && MET == 1 && m32 != nullptr; }
   // the team's FP32 staging vectors (shared memory, four of DENSE32_MAXD;
   // the dense32 steps that use them -- metric product, momentum solve,
   // Welford update -- never overlap)

@@ -532,6 +532,16 @@ int launch_glm(const GradOut& G, const DevModel& M, cudaStream_t st) {
 
 }  // namespace
 
+// a tensor-core kernel whose bounded pipeline wait ran out records it in its
+// plan's error flag (after a synchronisation)
+static int plan_timeout(const GradSetup& gs, std::string& err) {
+  if ((gs.plan && tc_error(gs.plan)) || (gs.wide && wide_error(gs.wide))) {
+    err = "tensor-core gradient: a bounded pipeline wait ran out";
+    return GNUTS_ERR_TIMEOUT;
+  }
+  return GNUTS_OK;
+}
+
 int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, double* dl, double* dg, int prec,
                           std::string& err) {
   if (M.K > 1024) { err = "batched gradient supports at most 1024 predictors"; return GNUTS_ERR_ARGUMENT; }
@@ -541,13 +551,13 @@ int batched_log_prob_grad(const DevModel& M, int n, const double* dq, int jac, d
   const int threads = 128, blocks = (n * 32 + threads - 1) / threads;
   k_stage_points<<<blocks, threads>>>(gs.G, M, n, dq);
   if (launch_glm(gs.G, M, 0)) {
-    err = "the batched gradient's GEMM could not be launched";
+    err = "the batched gradient could not be launched";
     return GNUTS_ERR_CUDA;
   }
   k_reduce_points<<<blocks, threads>>>(gs.G, M, n, dq, jac, dl, dg);
   GN_CUDA(cudaGetLastError());
   GN_CUDA(cudaDeviceSynchronize());
-  return GNUTS_OK;
+  return plan_timeout(gs, err);
 }
 
 // Hands completed draw rows to the caller's sink (gnuts_set_draw_sink) while
@@ -668,7 +678,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   GN_CUDA(cudaStreamEndCapture(stream, &graph));
   if (glm_rc) {
     cudaGraphDestroy(graph);
-    err = "the batched gradient's GEMM could not be captured";
+    err = "the batched gradient could not be captured";
     return GNUTS_ERR_CUDA;
   }
   GN_CUDA(cudaEventRecord(tev[3], stream));
@@ -693,7 +703,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
     if (timed) {
       GN_CUDA(cudaEventRecord(tev[0], stream));
       if (launch_glm(G, M, stream)) {
-        err = "the batched gradient's GEMM could not be launched";
+        err = "the batched gradient could not be launched";
         return GNUTS_ERR_CUDA;
       }
       GN_CUDA(cudaEventRecord(tev[1], stream));
@@ -743,10 +753,7 @@ static int run_rounds(Model& m, const Params& P, const Bufs& B, int prec, double
   }
   GN_CUDA(cudaEventRecord(tev[4], stream));
   GN_CUDA(cudaStreamSynchronize(stream));
-  if (gs.plan && tc_error(gs.plan)) {
-    err = "tensor-core gradient: a bounded pipeline wait ran out";
-    return GNUTS_ERR_TIMEOUT;
-  }
+  if ((st = plan_timeout(gs, err))) return st;
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
   float total_ms = 0;

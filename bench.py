@@ -438,7 +438,10 @@ def run_profile_case(case):
     flow_hier_256 - the learned sampler's fused kernel (flow trained 50 steps
     on the centered hierarchical model, then 256 chains x 20 + 10);
     horseshoe_short - the wide-design gradient round (horseshoe, 256 chains,
-    5 + 2, mixed precision)."""
+    5 + 2, mixed precision);
+    horseshoe_100k - the same on 100,000 rows (X 200 MB as BF16, larger than
+    L2; about 1.5 GB on the device), for full ncu captures of single
+    launches."""
     import cmdstan_gb300 as gn
     from cmdstan_gb300 import workloads
     if case == "flow_hier_256":
@@ -448,7 +451,8 @@ def run_profile_case(case):
         f.train(m, steps=50, seed=3)
         fit = m.sample_flow(f, num_chains=256, num_warmup=20, num_samples=10, seed=5)
     else:
-        m = gn.Model("horseshoe", workloads.horseshoe(seed=0))
+        n_rows = 100_000 if case == "horseshoe_100k" else 200_000
+        m = gn.Model("horseshoe", workloads.horseshoe(seed=0, N=n_rows))
         fit = m.sample(num_chains=256, num_warmup=5, num_samples=2, seed=3, precision=gn.PRECISION_MIXED, refresh=0)
     print(json.dumps({"profile_case": case, "note": "profiling run, not a bench value",
                       "timing": {k: float(v) for k, v in fit.timing.items()},
@@ -467,7 +471,7 @@ def main():
                     help="skip the batched-posterior and funnel (learned vs plain) workloads")
     ap.add_argument("--quick", action="store_true",
                     help="profiling aid: one short run (20 warmup + 10 draws) of the same workload; not a bench value")
-    ap.add_argument("--profile-case", choices=["flow_hier_256", "horseshoe_short"],
+    ap.add_argument("--profile-case", choices=["flow_hier_256", "horseshoe_short", "horseshoe_100k"],
                     help="profiling aid: a short run of another workload's hot kernel; not a bench value")
     args = ap.parse_args()
     if args.impl == "reference":

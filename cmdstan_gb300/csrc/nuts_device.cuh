@@ -79,10 +79,10 @@ constexpr int DENSE32_MAXD = 2048;
 constexpr int NCACHE_VEC = 17;
 constexpr int NCACHE_VEC_DIAG = 20;
 // elements per lane whose loads are issued together: VCH in the record
-// loops (merge, finish_doubling: nine or ten vectors), VCW in the loops over
-// at most four vectors (leapfrog, leaf record, dot, metric product, copies)
+// loops (merge, finish_doubling: nine or ten vectors), Chain::VCW in the
+// loops over at most four vectors (leapfrog, leaf record, dot, metric
+// product, copies)
 constexpr int VCH = 4;
-constexpr int VCW = 8;
 constexpr int VC1 = 4;  // elements per lane of the one-pass leaf step (D <= 128)
 
 struct Bufs {
@@ -147,6 +147,11 @@ __device__ __forceinline__ void ff_axpy(float& hi_io, float& lo_io, float a0, fl
 
 template <int MET = -1, int TW = 32>
 struct Chain {
+  // chunk of the loops over at most four vectors: 4 elements per lane for a
+  // warp (D up to about 128: less masked FP64 work per chunk), 8 for a team
+  // (a wide chain's 16 elements per thread in two chunks).  Each lane visits
+  // its elements in increasing order either way, so sums do not change.
+  static constexpr int VCW = TW == 32 ? 4 : 8;
   const Params& P;
   const Bufs& B;
   const DevModel& M;
